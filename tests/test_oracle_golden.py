@@ -1,0 +1,54 @@
+"""Pin the CPU oracle against vectors produced by the reference's own code.
+
+The fixtures come from tests/golden/make_golden.py, which runs the reference
+cutc_int path (src/cutc_int.c and the kernels it launches) compiled for the
+CPU.  The pair terms must agree bit for bit; the contracted outputs differ only
+by the summation order of the DGEMMs.
+"""
+import numpy as np
+import pytest
+
+from golden_util import CASE_NAMES, load_case, load_small_digest
+from oracle import oracle
+from cutc_gb300 import synth
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_pair_bit_exact(name):
+    p, ref = load_case(name)
+    G = oracle.pair(p)
+    assert np.array_equal(G, ref["G"])
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_cutc_int_matches_reference(name):
+    p, ref = load_case(name)
+    X3, A = oracle.cutc_int(p)
+    ex = oracle.rel_err(X3, ref["X"])
+    ei = oracle.rel_err(A, ref["int2e"])
+    assert ex["norm"] < 1e-13 and ex["max"] < 1e-13, ex
+    assert ei["norm"] < 1e-13 and ei["max"] < 1e-13, ei
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_blocked_oracle_is_block_invariant(name):
+    p, ref = load_case(name)
+    X3a, Aa = oracle.cutc_int(p)
+    X3b, Ab = oracle.cutc_int(p, block1=7)
+    assert oracle.rel_err(X3b, X3a)["max"] < 1e-14
+    assert oracle.rel_err(Ab, Aa)["max"] < 1e-13
+
+
+def test_small_workload_digest():
+    d = load_small_digest()
+    p = synth.make_config("small")
+    from golden_util import GOLDEN  # noqa: F401
+    from tests_inputs import input_checksums
+    cs = input_checksums(p)
+    np.testing.assert_allclose(cs, d["input_checksums"], rtol=1e-12, atol=1e-12)
+    X3, A = oracle.cutc_int(p)
+    xm, im = float(d["X_max"]), float(d["I_max"])
+    assert np.max(np.abs(X3.ravel()[d["X_idx"]] - d["X_val"])) < 1e-12 * xm
+    assert np.max(np.abs(A.ravel()[d["I_idx"]] - d["I_val"])) < 1e-12 * im
+    assert abs(np.linalg.norm(X3.ravel()) - d["X_norm"]) < 1e-12 * d["X_norm"]
+    assert abs(np.linalg.norm(A.ravel()) - d["I_norm"]) < 1e-12 * d["I_norm"]
