@@ -1,0 +1,164 @@
+"""GB300-native transcorrelated-integral engine (drop-in for CuTC's cutc_int).
+
+The compute path is the CUDA library ``cutc_gb300/lib/libcutcint.so`` (sm_103a),
+reached through its C-ABI (include/cutc_int.h) with ctypes.  This module
+mirrors the reference's entry point -- same name, argument order, array
+layouts and return codes as ``cutc_int`` (src/cutc_int.c:15-20) -- and adds
+the extended options.  There is no CPU fallback: if the library cannot be
+loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libcutcint.so")
+
+CUTC_OK = 0
+CUTC_ERR_LAUNCH_DIMS = -1
+CUTC_ERR_INVALID = -2
+CUTC_ERR_NO_MEMORY = -3
+CUTC_ERR_CUDA = -4
+CUTC_ERR_NO_DEVICE = -5
+CUTC_ERR_TIMEOUT = -6
+
+PLAIN_FP64 = 0
+SPLIT_BF16 = 1
+
+# every symbol include/cutc_int.h declares
+EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_default_options", "cutc_jast_bh_dev",
+           "cutc_validate_launch_dims", "cutc_last_error", "cutc_release"]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("n_slices", ctypes.c_int),
+                ("a_en", ctypes.c_double), ("a_ee", ctypes.c_double),
+                ("x_components", ctypes.c_int), ("device_pointers", ctypes.c_int),
+                ("max_work_bytes", ctypes.c_size_t), ("stream", ctypes.c_void_p)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("ms_total", ctypes.c_double), ("ms_h2d", ctypes.c_double),
+                ("ms_pair", ctypes.c_double), ("ms_x", ctypes.c_double),
+                ("ms_int2e", ctypes.c_double), ("ms_d2h", ctypes.c_double),
+                ("n_r1_tiles", ctypes.c_int), ("gpu_launches", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class CutcError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("cutc status %d: %s" % (status, message))
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libcutcint.so (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        from . import build as _build
+        _build.build()
+    L = ctypes.CDLL(path)
+    i, vp, dp = ctypes.c_int, ctypes.c_void_p, ctypes.c_double
+    L.cutc_int.argtypes = [i] * 11 + [vp] * 13
+    L.cutc_int.restype = i
+    L.cutc_int_ex.argtypes = [ctypes.POINTER(Options)] + [i] * 5 + [vp] * 13 + [ctypes.POINTER(Stats)]
+    L.cutc_int_ex.restype = i
+    L.cutc_default_options.argtypes = [ctypes.POINTER(Options)]
+    L.cutc_default_options.restype = None
+    L.cutc_jast_bh_dev.argtypes = [i] * 6 + [vp] * 7 + [dp, dp, vp]
+    L.cutc_jast_bh_dev.restype = i
+    L.cutc_validate_launch_dims.argtypes = [i] * 6
+    L.cutc_validate_launch_dims.restype = i
+    L.cutc_last_error.argtypes = []
+    L.cutc_last_error.restype = ctypes.c_char_p
+    L.cutc_release.argtypes = []
+    L.cutc_release.restype = None
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return load().cutc_last_error().decode()
+
+
+def _vp(a):
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    assert a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def cutc_int(nxBlocks, nyBlocks, nzBlocks, blockxSize, blockySize, blockzSize,
+             n_grid1, n_grid2, n_ao, n_nuc, size_bh,
+             r1, wr1, r2, wr2, rn, aos_data1, aos_data2,
+             c_bh, m_bh, n_bh, o_bh, int2_grad1_u12_ao, int_2e_ao) -> int:
+    """The reference entry point: host arrays in, host outputs filled, status out."""
+    L = load()
+    arrs = [r1, wr1, r2, wr2, rn, aos_data1, aos_data2, c_bh, m_bh, n_bh, o_bh,
+            int2_grad1_u12_ao, int_2e_ao]
+    return L.cutc_int(nxBlocks, nyBlocks, nzBlocks, blockxSize, blockySize, blockzSize,
+                      n_grid1, n_grid2, n_ao, n_nuc, size_bh, *[_vp(a) for a in arrs])
+
+
+def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_components=3,
+            device_pointers=False, max_work_bytes=0, stream=None) -> Options:
+    o = Options()
+    load().cutc_default_options(ctypes.byref(o))
+    o.precision = precision
+    if n_slices is not None:
+        o.n_slices = n_slices
+    o.a_en, o.a_ee = a_en, a_ee
+    o.x_components = x_components
+    o.device_pointers = 1 if device_pointers else 0
+    o.max_work_bytes = max_work_bytes
+    o.stream = stream
+    return o
+
+
+def cutc_int_ex(opt: Options, n_grid1, n_grid2, n_ao, n_nuc, size_bh,
+                r1, wr1, r2, wr2, rn, aos_data1, aos_data2, c_bh, m_bh, n_bh, o_bh,
+                X, I, stats: Stats | None = None) -> int:
+    L = load()
+    arrs = [r1, wr1, r2, wr2, rn, aos_data1, aos_data2, c_bh, m_bh, n_bh, o_bh, X, I]
+    return L.cutc_int_ex(ctypes.byref(opt), n_grid1, n_grid2, n_ao, n_nuc, size_bh,
+                         *[_vp(a) for a in arrs], ctypes.byref(stats) if stats is not None else None)
+
+
+def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
+                    max_work_bytes=0, with_stats=False):
+    """Host-array convenience call on a synth.Problem: returns (X, int_2e[, stats]).
+
+    X is (x_components, n1, nA^2) == Fortran (nA, nA, n1, comps); int_2e is
+    (nA^2, nA^2) == Fortran (nA, nA, nA, nA).
+    """
+    X = np.empty((x_components, p.n_grid1, p.n_ao ** 2))
+    I = np.empty((p.n_ao ** 2, p.n_ao ** 2))
+    st = Stats()
+    opt = options(precision, n_slices, p.a_en, p.a_ee, x_components, False, max_work_bytes)
+    s = cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                    p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2,
+                    p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I, st)
+    if s != CUTC_OK:
+        raise CutcError(s, last_error())
+    return (X, I, st.as_dict()) if with_stats else (X, I)
+
+
+def jast_bh_device(r1, r2, rn, c_bh, m_bh, n_bh, o_bh, G, i0=0, n1b=None,
+                   a_en=1.0, a_ee=1.0) -> int:
+    """Pair terms on device tensors (torch, float64/int32, contiguous)."""
+    n1 = r1.shape[0]
+    n1b = n1 - i0 if n1b is None else n1b
+    L = load()
+    return L.cutc_jast_bh_dev(i0, n1b, n1, r2.shape[0], rn.shape[0], c_bh.shape[1],
+                              _vp(r1), _vp(r2), _vp(rn), _vp(c_bh), _vp(m_bh), _vp(n_bh),
+                              _vp(o_bh), a_en, a_ee, _vp(G))

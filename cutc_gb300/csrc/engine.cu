@@ -1,0 +1,594 @@
+// Host orchestration of one integral build on one GPU (sm_103a).
+//
+// Counterpart of the reference's host drivers src/cutc_int.c:15-243,
+// src/build_int2_grad1_u12_ao.cu:9-347 and src/build_int_2e_ao.cu:11-145,
+// redesigned:
+//   * one engine per device with its own stream, cuBLAS handle and a
+//     grow-only workspace (no cudaMalloc/cudaFree per call, no
+//     cudaDeviceSynchronize between steps: everything is stream-ordered);
+//   * r1 is tiled by a byte budget in 64-bit arithmetic (the reference sizes
+//     tiles in 32-bit int and from bytes instead of doubles);
+//   * the AO-pair products are packed (symmetric / antisymmetric halves), so
+//     both contractions do half (X) and a quarter (int_2e) of the dense work;
+//   * X is accumulated per r1 tile with beta = 0, so r1 tiling is exact (the
+//     reference keeps beta = 1 across r1 passes, src/build_int2_grad1_u12_ao.cu:166);
+//   * errors are returned as status codes, never exit().
+#include <cublas_v2.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.cuh"
+#include "pair.cuh"
+#include "products.cuh"
+#include "split.cuh"
+
+static thread_local char g_err[512] = "";
+
+void cutc_set_error(int status, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    int n = snprintf(g_err, sizeof(g_err), "[status %d] ", status);
+    if (n < 0)
+        n = 0;
+    vsnprintf(g_err + n, sizeof(g_err) - (size_t)n, fmt, ap);
+    va_end(ap);
+}
+
+extern "C" const char *cutc_last_error(void) { return g_err; }
+
+namespace cutc {
+
+static std::atomic<long> g_launches{0};
+void note_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
+
+#define CUBLAS_TRY(expr)                                                              \
+    do {                                                                              \
+        cublasStatus_t s_ = (expr);                                                   \
+        if (s_ != CUBLAS_STATUS_SUCCESS) {                                            \
+            cutc_set_error(CUTC_ERR_CUDA, "%s:%d %s: cuBLAS status %d", __FILE__,     \
+                           __LINE__, #expr, (int)s_);                                 \
+            return s_ == CUBLAS_STATUS_ALLOC_FAILED ? CUTC_ERR_NO_MEMORY : CUTC_ERR_CUDA; \
+        }                                                                             \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// engine and workspace
+// ---------------------------------------------------------------------------
+
+int Workspace::get(int slot, size_t bytes, void **out)
+{
+    if (slot >= (int)bufs.size())
+        bufs.resize(slot + 1);
+    Buf &b = bufs[slot];
+    bytes = (bytes + 255) & ~(size_t)255;
+    if (bytes == 0)
+        bytes = 256;
+    if (b.cap < bytes) {
+        if (b.p) {
+            cudaFree(b.p);
+            b.p = nullptr;
+            b.cap = 0;
+        }
+        cudaError_t e = cudaMalloc(&b.p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cutc_set_error(CUTC_ERR_NO_MEMORY, "cudaMalloc(%zu) for workspace slot %d: %s", bytes,
+                           slot, cudaGetErrorString(e));
+            return CUTC_ERR_NO_MEMORY;
+        }
+        b.cap = bytes;
+    }
+    *out = b.p;
+    return CUTC_OK;
+}
+
+void Workspace::release()
+{
+    for (auto &b : bufs)
+        if (b.p)
+            cudaFree(b.p);
+    bufs.clear();
+}
+
+static std::mutex g_engines_mu;
+static std::vector<Engine *> g_engines;
+
+int get_engine(Engine **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cutc_set_error(CUTC_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+        return CUTC_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> lk(g_engines_mu);
+    if ((int)g_engines.size() <= dev)
+        g_engines.resize(dev + 1, nullptr);
+    if (!g_engines[dev]) {
+        cudaDeviceProp prop;
+        CUTC_CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
+        if (prop.major != 10 || prop.minor != 3) {
+            cutc_set_error(CUTC_ERR_NO_DEVICE,
+                           "device %d is sm_%d%d; this library is built for sm_103a (GB300)", dev,
+                           prop.major, prop.minor);
+            return CUTC_ERR_NO_DEVICE;
+        }
+        Engine *E = new Engine();
+        E->device = dev;
+        E->n_sm = prop.multiProcessorCount;
+        E->max_threads_per_block = prop.maxThreadsPerBlock;
+        for (int k = 0; k < 3; k++)
+            E->max_grid[k] = prop.maxGridSize[k];
+        CUTC_CUDA_TRY(cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking));
+        if (cublasCreate(&E->blas) != CUBLAS_STATUS_SUCCESS) {
+            cutc_set_error(CUTC_ERR_CUDA, "cublasCreate failed");
+            return CUTC_ERR_CUDA;
+        }
+        for (int k = 0; k < kNumEvents; k++)
+            CUTC_CUDA_TRY(cudaEventCreate(&E->ev[k]));
+        g_engines[dev] = E;
+    }
+    *out = g_engines[dev];
+    return CUTC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// request preparation
+// ---------------------------------------------------------------------------
+
+int build_terms(const Request &R, std::vector<double> &coef, std::vector<int> &exps,
+                std::vector<int> &off)
+{
+    coef.clear();
+    exps.clear();
+    off.assign(R.nN + 1, 0);
+    for (int A = 0; A < R.nN; A++) {
+        off[A] = (int)exps.size();
+        for (int p = 0; p < R.nB; p++) {
+            const int k = p + R.nB * A;  // Fortran (size_bh, n_nuc)
+            const int m = R.m_bh[k], n = R.n_bh[k], o = R.o_bh[k];
+            if (m < 0 || m > kMaxExp || n < 0 || n > kMaxExp || o < 0 || o > kMaxExp) {
+                cutc_set_error(CUTC_ERR_INVALID,
+                               "Jastrow exponent out of [0, %d] at term %d of nucleus %d "
+                               "(m=%d n=%d o=%d)", kMaxExp, p, A, m, n, o);
+                return CUTC_ERR_INVALID;
+            }
+            const double c = R.c_bh[k];
+            if (!(std::fabs(c) >= 1e-10))  // skipped like src/jast_bh.cu:203 (NaN skipped too)
+                continue;
+            coef.push_back(c * m);
+            coef.push_back(c * n);
+            coef.push_back(c * o);
+            exps.push_back(m | (n << 3) | (o << 6));
+        }
+    }
+    off[R.nN] = (int)exps.size();
+    if ((int)exps.size() > kMaxTerms) {
+        cutc_set_error(CUTC_ERR_INVALID, "%d Jastrow terms exceed the limit %d", (int)exps.size(),
+                       kMaxTerms);
+        return CUTC_ERR_INVALID;
+    }
+    return CUTC_OK;
+}
+
+static int validate(const Request &R)
+{
+    if (R.n1 <= 0 || R.n2 <= 0 || R.nA <= 0 || R.nN <= 0 || R.nB < 0) {
+        cutc_set_error(CUTC_ERR_INVALID, "sizes must be positive (n_grid1=%d n_grid2=%d n_ao=%d "
+                       "n_nuc=%d size_bh=%d)", R.n1, R.n2, R.nA, R.nN, R.nB);
+        return CUTC_ERR_INVALID;
+    }
+    if (R.nN > kMaxNuc) {
+        cutc_set_error(CUTC_ERR_INVALID, "n_nuc=%d exceeds %d", R.nN, kMaxNuc);
+        return CUTC_ERR_INVALID;
+    }
+    if ((int64_t)R.nA * R.nA > (int64_t)INT32_MAX / 2) {
+        cutc_set_error(CUTC_ERR_INVALID, "n_ao=%d too large", R.nA);
+        return CUTC_ERR_INVALID;
+    }
+    const void *ptrs[] = {R.r1, R.wr1, R.r2, R.wr2, R.rn, R.aos1, R.aos2, R.X, R.I};
+    for (const void *p : ptrs)
+        if (!p) {
+            cutc_set_error(CUTC_ERR_INVALID, "NULL array argument");
+            return CUTC_ERR_INVALID;
+        }
+    if (R.nB > 0 && (!R.c_bh || !R.m_bh || !R.n_bh || !R.o_bh)) {
+        cutc_set_error(CUTC_ERR_INVALID, "NULL Jastrow parameter array");
+        return CUTC_ERR_INVALID;
+    }
+    if (!(R.a_en > 0.0) || !(R.a_ee > 0.0)) {
+        cutc_set_error(CUTC_ERR_INVALID, "a_en and a_ee must be positive");
+        return CUTC_ERR_INVALID;
+    }
+    if (R.x_components != 3 && R.x_components != 4) {
+        cutc_set_error(CUTC_ERR_INVALID, "x_components must be 3 or 4");
+        return CUTC_ERR_INVALID;
+    }
+    if (R.precision != CUTC_PLAIN_FP64 && R.precision != CUTC_SPLIT_BF16) {
+        cutc_set_error(CUTC_ERR_INVALID, "unknown precision form %d", R.precision);
+        return CUTC_ERR_INVALID;
+    }
+    if (R.precision == CUTC_SPLIT_BF16 && (R.n_slices < 3 || R.n_slices > kMaxSlices)) {
+        cutc_set_error(CUTC_ERR_INVALID, "n_slices must be in [3, %d]", kMaxSlices);
+        return CUTC_ERR_INVALID;
+    }
+    return CUTC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the build
+// ---------------------------------------------------------------------------
+
+enum Slot {
+    S_R1, S_WR1, S_R2, S_WR2, S_RN, S_AOS1, S_AOS2, S_COEF, S_EXPS, S_OFF,
+    S_T1, S_F2, S_P, S_G, S_XP, S_S0, S_SL, S_H, S_N, S_XOUT, S_IOUT,
+    S_SPLIT0  // split-form slots follow
+};
+
+static inline double ev_ms(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+// Bytes per r1 row of the X-build working set (G tile, plus slices when split).
+static size_t r1_row_bytes(const Request &R)
+{
+    size_t g = 4 * (size_t)R.n2 * sizeof(double);
+    if (R.precision == CUTC_SPLIT_BF16)
+        g += split_r1_row_bytes(R);
+    return g;
+}
+
+int run_build(Engine *E, const Request &R, cutc_stats *stats)
+{
+    CUTC_TRY(validate(R));
+    std::vector<double> coef;
+    std::vector<int> exps, off;
+    CUTC_TRY(build_terms(R, coef, exps, off));
+
+    cudaStream_t st = R.stream ? R.stream : E->stream;
+    Workspace &W = E->ws;
+    const int n1 = R.n1, n2 = R.n2, nA = R.nA, nN = R.nN;
+    const int64_t np = n_pairs(nA), nl = n_strict_pairs(nA), nA2 = (int64_t)nA * nA;
+    const long launches0 = launches_so_far();
+
+    CUTC_CUDA_TRY(cudaEventRecord(E->ev[0], st));
+
+    // ---- inputs on the device --------------------------------------------
+    const double *d_r1, *d_wr1, *d_r2, *d_wr2, *d_rn, *d_aos1, *d_aos2v;
+    double *d_X, *d_I;
+    void *p;
+    auto put = [&](int slot, const void *h, size_t bytes, const double **dst) -> int {
+        CUTC_TRY(W.get(slot, bytes, &p));
+        CUTC_CUDA_TRY(cudaMemcpyAsync(p, h, bytes, cudaMemcpyHostToDevice, st));
+        *dst = (const double *)p;
+        return CUTC_OK;
+    };
+    if (R.device_pointers) {
+        d_r1 = R.r1; d_wr1 = R.wr1; d_r2 = R.r2; d_wr2 = R.wr2; d_rn = R.rn;
+        d_aos1 = R.aos1;
+        d_aos2v = R.aos2;  // component 0 is the first n2*nA block
+        d_X = R.X;
+        d_I = R.I;
+    } else {
+        CUTC_TRY(put(S_R1, R.r1, 3 * (size_t)n1 * 8, &d_r1));
+        CUTC_TRY(put(S_WR1, R.wr1, (size_t)n1 * 8, &d_wr1));
+        CUTC_TRY(put(S_R2, R.r2, 3 * (size_t)n2 * 8, &d_r2));
+        CUTC_TRY(put(S_WR2, R.wr2, (size_t)n2 * 8, &d_wr2));
+        CUTC_TRY(put(S_RN, R.rn, 3 * (size_t)nN * 8, &d_rn));
+        CUTC_TRY(put(S_AOS1, R.aos1, 4 * (size_t)n1 * nA * 8, &d_aos1));
+        // only the value component of aos_data2 is used (src/long_range_integ.cu:30-35)
+        CUTC_TRY(put(S_AOS2, R.aos2, (size_t)n2 * nA * 8, &d_aos2v));
+        CUTC_TRY(W.get(S_XOUT, (size_t)R.x_components * n1 * nA2 * 8, &p));
+        d_X = (double *)p;
+        CUTC_TRY(W.get(S_IOUT, (size_t)nA2 * nA2 * 8, &p));
+        d_I = (double *)p;
+    }
+    const int nt = (int)exps.size();
+    double *d_coef;
+    int *d_exps, *d_off;
+    CUTC_TRY(W.get(S_COEF, std::max<size_t>(1, coef.size()) * 8, &p));
+    d_coef = (double *)p;
+    CUTC_TRY(W.get(S_EXPS, std::max<size_t>(1, exps.size()) * 4, &p));
+    d_exps = (int *)p;
+    CUTC_TRY(W.get(S_OFF, off.size() * 4, &p));
+    d_off = (int *)p;
+    if (nt) {
+        CUTC_CUDA_TRY(cudaMemcpyAsync(d_coef, coef.data(), coef.size() * 8, cudaMemcpyHostToDevice, st));
+        CUTC_CUDA_TRY(cudaMemcpyAsync(d_exps, exps.data(), exps.size() * 4, cudaMemcpyHostToDevice, st));
+    }
+    CUTC_CUDA_TRY(cudaMemcpyAsync(d_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice, st));
+    CUTC_CUDA_TRY(cudaEventRecord(E->ev[1], st));
+
+    // ---- r1 tiling ---------------------------------------------------------
+    size_t budget = R.max_work_bytes;
+    if (budget == 0) {
+        size_t free_b = 0, total_b = 0;
+        CUTC_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+        budget = std::min<size_t>((size_t)24 << 30, free_b / 3);
+    }
+    int64_t n1t = (int64_t)(budget / r1_row_bytes(R));
+    n1t = std::max<int64_t>(1, std::min<int64_t>(n1t, n1));
+    if (R.tile_rows > 0)
+        n1t = std::min<int64_t>(n1t, R.tile_rows);
+    const int n_tiles = (int)((n1 + n1t - 1) / n1t);
+
+    // ---- per-point and pair-product terms -----------------------------------
+    NucTerm *d_t1;
+    double *d_f2, *d_P, *d_G, *d_Xp;
+    CUTC_TRY(W.get(S_T1, (size_t)n1t * nN * sizeof(NucTerm), &p));
+    d_t1 = (NucTerm *)p;
+    CUTC_TRY(W.get(S_F2, (size_t)nN * n2 * 8, &p));
+    d_f2 = (double *)p;
+    CUTC_TRY(W.get(S_G, 4 * (size_t)n1t * n2 * 8, &p));
+    d_G = (double *)p;
+    CUTC_TRY(W.get(S_XP, 4 * (size_t)n1 * np * 8, &p));
+    d_Xp = (double *)p;
+    CUTC_TRY(launch_r2_terms(st, n2, nN, d_r2, d_rn, R.a_en, d_f2));
+    note_launches(1);
+
+    SplitPlan sp;
+    if (R.precision == CUTC_PLAIN_FP64) {
+        CUTC_TRY(W.get(S_P, (size_t)np * n2 * 8, &p));
+        d_P = (double *)p;
+        CUTC_TRY(launch_sym_products(st, n2, nA, d_wr2, d_aos2v, n2, d_P, n2));
+        note_launches(1);
+    } else {
+        CUTC_TRY(split_prepare_x(E, R, st, d_wr2, d_aos2v, n1t, S_SPLIT0, sp));
+    }
+    CUTC_CUDA_TRY(cudaEventRecord(E->ev[2], st));
+
+    // ---- X build, tile by tile ------------------------------------------------
+    double ms_pair = 0.0;
+    CUBLAS_TRY(cublasSetStream(E->blas, st));
+    for (int tile = 0; tile < n_tiles; tile++) {
+        const int i0 = (int)(tile * n1t);
+        const int nb = (int)std::min<int64_t>(n1t, n1 - i0);
+        CUTC_TRY(launch_r1_terms(st, i0, nb, nN, d_r1, d_rn, R.a_en, d_t1));
+        PairArgs P;
+        P.i0 = i0; P.n1b = nb; P.n2 = n2; P.nN = nN; P.n_terms = nt;
+        P.r1 = d_r1; P.r2 = d_r2; P.t1 = d_t1; P.f2 = d_f2;
+        P.coef = d_coef; P.exps = d_exps; P.term_off = d_off;
+        P.a_ee = R.a_ee;
+        P.G = d_G; P.ldg = n2; P.plane = (int64_t)nb * n2;
+        CUTC_CUDA_TRY(cudaEventRecord(E->ev[3], st));
+        CUTC_TRY(launch_pair_f64(st, P));
+        CUTC_CUDA_TRY(cudaEventRecord(E->ev[4], st));
+        note_launches(2);
+        if (R.precision == CUTC_PLAIN_FP64) {
+            // Xp[(m n1 + i0 + i) np + p] = sum_g P[p n2 + g] G[m plane + i n2 + g]
+            const double one = 1.0, zero = 0.0;
+            CUBLAS_TRY(cublasDgemmStridedBatched(
+                E->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)np, nb, n2, &one, d_P, n2, 0, d_G, n2,
+                (long long)nb * n2, &zero, d_Xp + (int64_t)i0 * np, (int)np,
+                (long long)n1 * np, 4));
+        } else {
+            CUTC_TRY(split_x_tile(E, R, st, sp, d_G, i0, nb, d_Xp));
+        }
+        if (stats) {
+            CUTC_CUDA_TRY(cudaEventSynchronize(E->ev[4]));
+            ms_pair += ev_ms(E->ev[3], E->ev[4]);
+        }
+    }
+    CUTC_CUDA_TRY(cudaEventRecord(E->ev[5], st));
+
+    // ---- int_2e -------------------------------------------------------------
+    if (R.precision == CUTC_PLAIN_FP64) {
+        double *d_S0, *d_Sl, *d_H, *d_N;
+        CUTC_TRY(W.get(S_S0, (size_t)np * n1 * 8, &p));
+        d_S0 = (double *)p;
+        CUTC_TRY(W.get(S_SL, (size_t)std::max<int64_t>(nl, 1) * 3 * n1 * 8, &p));
+        d_Sl = (double *)p;
+        CUTC_TRY(W.get(S_H, (size_t)np * np * 8, &p));
+        d_H = (double *)p;
+        CUTC_TRY(W.get(S_N, (size_t)np * std::max<int64_t>(nl, 1) * 8, &p));
+        d_N = (double *)p;
+        CUTC_TRY(launch_sym_products(st, n1, nA, d_wr1, d_aos1, n1, d_S0, n1));
+        CUTC_TRY(launch_antisym_products(st, n1, nA, d_wr1, d_aos1, d_Sl, 3 * (int64_t)n1));
+        note_launches(2);
+        const double one = 1.0, zero = 0.0, mhalf = -0.5;
+        // H = X_3 S0   (src/build_int_2e_ao.cu:60-67, packed)
+        CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)np, n1, &one,
+                               d_Xp + 3 * (int64_t)n1 * np, (int)np, d_S0, n1, &zero, d_H, (int)np));
+        // N = -1/2 [X_0 X_1 X_2] S   (src/build_int_2e_ao.cu:97-104, packed)
+        if (nl > 0)
+            CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)nl, 3 * n1,
+                                   &mhalf, d_Xp, (int)np, d_Sl, 3 * n1, &zero, d_N, (int)np));
+        CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, d_I));
+        note_launches(1);
+    } else {
+        CUTC_TRY(split_int2e(E, R, st, sp, d_wr1, d_aos1, d_Xp, d_I));
+    }
+    CUTC_CUDA_TRY(cudaEventRecord(E->ev[6], st));
+
+    // ---- X in the reference layout, outputs to the host -------------------------
+    CUTC_TRY(launch_expand_pairs(st, (int64_t)R.x_components * n1, nA, d_Xp, np, d_X));
+    note_launches(1);
+    CUTC_CUDA_TRY(cudaEventRecord(E->ev[7], st));
+    if (!R.device_pointers) {
+        CUTC_CUDA_TRY(cudaMemcpyAsync(R.X, d_X, (size_t)R.x_components * n1 * nA2 * 8,
+                                      cudaMemcpyDeviceToHost, st));
+        CUTC_CUDA_TRY(cudaMemcpyAsync(R.I, d_I, (size_t)nA2 * nA2 * 8, cudaMemcpyDeviceToHost, st));
+    }
+    CUTC_CUDA_TRY(cudaEventRecord(E->ev[8], st));
+    CUTC_CUDA_TRY(cudaEventSynchronize(E->ev[8]));
+    CUTC_CUDA_TRY(cudaGetLastError());
+
+    if (stats) {
+        stats->ms_h2d = ev_ms(E->ev[0], E->ev[1]);
+        stats->ms_pair = ms_pair;
+        stats->ms_x = ev_ms(E->ev[1], E->ev[5]) - ms_pair;
+        stats->ms_int2e = ev_ms(E->ev[5], E->ev[6]);
+        stats->ms_d2h = ev_ms(E->ev[7], E->ev[8]);
+        stats->ms_total = ev_ms(E->ev[0], E->ev[8]);
+        stats->n_r1_tiles = n_tiles;
+        stats->gpu_launches = (int)(launches_so_far() - launches0);
+    }
+    return CUTC_OK;
+}
+
+int run_pair_only(Engine *E, int i0, int n1b, int n1, int n2, int nN, int nB, const double *r1,
+                  const double *r2, const double *rn, const double *c_bh, const int *m_bh,
+                  const int *n_bh, const int *o_bh, double a_en, double a_ee, double *G)
+{
+    if (n1b <= 0 || n2 <= 0 || nN <= 0 || nB < 0 || i0 < 0 || i0 + n1b > n1 || nN > kMaxNuc ||
+        !r1 || !r2 || !rn || !G || !(a_en > 0) || !(a_ee > 0)) {
+        cutc_set_error(CUTC_ERR_INVALID, "invalid pair-kernel arguments");
+        return CUTC_ERR_INVALID;
+    }
+    // parameters come from the device: bring them to the host to build the term table
+    std::vector<double> c((size_t)nN * nB);
+    std::vector<int> m((size_t)nN * nB), n((size_t)nN * nB), o((size_t)nN * nB);
+    cudaStream_t st = E->stream;
+    if (nB > 0) {
+        CUTC_CUDA_TRY(cudaMemcpyAsync(c.data(), c_bh, c.size() * 8, cudaMemcpyDeviceToHost, st));
+        CUTC_CUDA_TRY(cudaMemcpyAsync(m.data(), m_bh, m.size() * 4, cudaMemcpyDeviceToHost, st));
+        CUTC_CUDA_TRY(cudaMemcpyAsync(n.data(), n_bh, n.size() * 4, cudaMemcpyDeviceToHost, st));
+        CUTC_CUDA_TRY(cudaMemcpyAsync(o.data(), o_bh, o.size() * 4, cudaMemcpyDeviceToHost, st));
+        CUTC_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    Request R{};
+    R.nN = nN; R.nB = nB; R.c_bh = c.data(); R.m_bh = m.data(); R.n_bh = n.data(); R.o_bh = o.data();
+    std::vector<double> coef;
+    std::vector<int> exps, off;
+    CUTC_TRY(build_terms(R, coef, exps, off));
+    Workspace &W = E->ws;
+    void *p;
+    CUTC_TRY(W.get(S_COEF, std::max<size_t>(1, coef.size()) * 8, &p));
+    double *d_coef = (double *)p;
+    CUTC_TRY(W.get(S_EXPS, std::max<size_t>(1, exps.size()) * 4, &p));
+    int *d_exps = (int *)p;
+    CUTC_TRY(W.get(S_OFF, off.size() * 4, &p));
+    int *d_off = (int *)p;
+    if (!exps.empty()) {
+        CUTC_CUDA_TRY(cudaMemcpyAsync(d_coef, coef.data(), coef.size() * 8, cudaMemcpyHostToDevice, st));
+        CUTC_CUDA_TRY(cudaMemcpyAsync(d_exps, exps.data(), exps.size() * 4, cudaMemcpyHostToDevice, st));
+    }
+    CUTC_CUDA_TRY(cudaMemcpyAsync(d_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice, st));
+    CUTC_TRY(W.get(S_T1, (size_t)n1b * nN * sizeof(NucTerm), &p));
+    NucTerm *d_t1 = (NucTerm *)p;
+    CUTC_TRY(W.get(S_F2, (size_t)nN * n2 * 8, &p));
+    double *d_f2 = (double *)p;
+    CUTC_TRY(launch_r1_terms(st, i0, n1b, nN, r1, rn, a_en, d_t1));
+    CUTC_TRY(launch_r2_terms(st, n2, nN, r2, rn, a_en, d_f2));
+    PairArgs P;
+    P.i0 = i0; P.n1b = n1b; P.n2 = n2; P.nN = nN; P.n_terms = (int)exps.size();
+    P.r1 = r1; P.r2 = r2; P.t1 = d_t1; P.f2 = d_f2;
+    P.coef = d_coef; P.exps = d_exps; P.term_off = d_off; P.a_ee = a_ee;
+    P.G = G; P.ldg = n2; P.plane = (int64_t)n1b * n2;
+    CUTC_TRY(launch_pair_f64(st, P));
+    note_launches(3);
+    CUTC_CUDA_TRY(cudaStreamSynchronize(st));
+    return CUTC_OK;
+}
+
+}  // namespace cutc
+
+// ---------------------------------------------------------------------------
+// C-ABI
+// ---------------------------------------------------------------------------
+using namespace cutc;
+
+extern "C" void cutc_default_options(cutc_options *opt)
+{
+    memset(opt, 0, sizeof(*opt));
+    opt->precision = CUTC_PLAIN_FP64;
+    opt->n_slices = kDefaultSlices;
+    opt->a_en = 1.0;
+    opt->a_ee = 1.0;
+    opt->x_components = 3;
+}
+
+extern "C" int cutc_int_ex(const cutc_options *opt, int n_grid1, int n_grid2, int n_ao, int n_nuc,
+                           int size_bh, const double *r1, const double *wr1, const double *r2,
+                           const double *wr2, const double *rn, const double *aos_data1,
+                           const double *aos_data2, const double *c_bh, const int *m_bh,
+                           const int *n_bh, const int *o_bh, double *int2_grad1_u12_ao,
+                           double *int_2e_ao, cutc_stats *stats)
+{
+    cutc_options defaults;
+    if (!opt) {
+        cutc_default_options(&defaults);
+        opt = &defaults;
+    }
+    Engine *E = nullptr;
+    CUTC_TRY(get_engine(&E));
+    Request R{};
+    R.precision = opt->precision;
+    R.n_slices = opt->n_slices;
+    R.a_en = opt->a_en;
+    R.a_ee = opt->a_ee;
+    R.x_components = opt->x_components;
+    R.device_pointers = opt->device_pointers;
+    R.max_work_bytes = opt->max_work_bytes;
+    R.stream = (cudaStream_t)opt->stream;
+    R.n1 = n_grid1; R.n2 = n_grid2; R.nA = n_ao; R.nN = n_nuc; R.nB = size_bh;
+    R.r1 = r1; R.wr1 = wr1; R.r2 = r2; R.wr2 = wr2; R.rn = rn;
+    R.aos1 = aos_data1; R.aos2 = aos_data2;
+    R.c_bh = c_bh; R.m_bh = m_bh; R.n_bh = n_bh; R.o_bh = o_bh;
+    R.X = int2_grad1_u12_ao; R.I = int_2e_ao;
+    const char *tr = getenv("CUTC_TILE_ROWS");
+    R.tile_rows = tr ? atoi(tr) : 0;
+    if (stats)
+        memset(stats, 0, sizeof(*stats));
+    std::lock_guard<std::mutex> lk(E->mu);
+    int s = run_build(E, R, stats);
+    if (s != CUTC_OK)
+        cudaStreamSynchronize(R.stream ? R.stream : E->stream);
+    return s;
+}
+
+extern "C" int cutc_jast_bh_dev(int i0, int n1b, int n_grid1, int n_grid2, int n_nuc, int size_bh,
+                                const double *r1, const double *r2, const double *rn,
+                                const double *c_bh, const int *m_bh, const int *n_bh,
+                                const int *o_bh, double a_en, double a_ee, double *grad1u)
+{
+    Engine *E = nullptr;
+    CUTC_TRY(get_engine(&E));
+    std::lock_guard<std::mutex> lk(E->mu);
+    return run_pair_only(E, i0, n1b, n_grid1, n_grid2, n_nuc, size_bh, r1, r2, rn, c_bh, m_bh,
+                         n_bh, o_bh, a_en, a_ee, grad1u);
+}
+
+extern "C" int cutc_validate_launch_dims(int gx, int gy, int gz, int bx, int by, int bz)
+{
+    Engine *E = nullptr;
+    CUTC_TRY(get_engine(&E));
+    // The reference compares unsigned dim3 products with the device limits
+    // (src/cutc_int.c:79-86); the same unsigned arithmetic is kept here.
+    const unsigned vol = (unsigned)bx * (unsigned)by * (unsigned)bz;
+    if (vol > (unsigned)E->max_threads_per_block) {
+        cutc_set_error(CUTC_ERR_LAUNCH_DIMS, "Too many threads per block");
+        return CUTC_ERR_LAUNCH_DIMS;
+    }
+    if ((unsigned)gx > (unsigned)E->max_grid[0] || (unsigned)gy > (unsigned)E->max_grid[1] ||
+        (unsigned)gz > (unsigned)E->max_grid[2]) {
+        cutc_set_error(CUTC_ERR_LAUNCH_DIMS, "Grid dimensions exceed device capabilities");
+        return CUTC_ERR_LAUNCH_DIMS;
+    }
+    return CUTC_OK;
+}
+
+extern "C" void cutc_release(void)
+{
+    Engine *E = nullptr;
+    if (get_engine(&E) != CUTC_OK)
+        return;
+    std::lock_guard<std::mutex> lk(E->mu);
+    cudaStreamSynchronize(E->stream);
+    E->ws.release();
+}

@@ -1,0 +1,64 @@
+// Engine context, workspace and request description (host side).
+#pragma once
+
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <vector>
+
+#include "cutc_int.h"
+
+namespace cutc {
+
+constexpr int kNumEvents = 12;
+
+// Grow-only device buffers, one per slot, reused across calls.
+struct Workspace {
+    struct Buf {
+        void *p = nullptr;
+        size_t cap = 0;
+    };
+    std::vector<Buf> bufs;
+    int get(int slot, size_t bytes, void **out);
+    void release();
+};
+
+struct Engine {
+    int device = 0;
+    int n_sm = 0;
+    int max_threads_per_block = 1024;
+    int max_grid[3] = {0, 0, 0};
+    cudaStream_t stream = nullptr;
+    cublasHandle_t blas = nullptr;
+    cudaEvent_t ev[kNumEvents];
+    Workspace ws;
+    std::mutex mu;
+};
+
+// One integral build, in the reference's argument layout.
+struct Request {
+    int precision = CUTC_PLAIN_FP64;
+    int n_slices = 5;
+    double a_en = 1.0, a_ee = 1.0;
+    int x_components = 3;
+    int device_pointers = 0;
+    size_t max_work_bytes = 0;
+    int tile_rows = 0;  // optional cap on r1 rows per tile
+    cudaStream_t stream = nullptr;
+    int n1 = 0, n2 = 0, nA = 0, nN = 0, nB = 0;
+    const double *r1 = nullptr, *wr1 = nullptr, *r2 = nullptr, *wr2 = nullptr, *rn = nullptr;
+    const double *aos1 = nullptr, *aos2 = nullptr;
+    const double *c_bh = nullptr;
+    const int *m_bh = nullptr, *n_bh = nullptr, *o_bh = nullptr;
+    double *X = nullptr, *I = nullptr;
+};
+
+int get_engine(Engine **out);
+int build_terms(const Request &R, std::vector<double> &coef, std::vector<int> &exps,
+                std::vector<int> &off);
+int run_build(Engine *E, const Request &R, cutc_stats *stats);
+void note_launches(int n);
+long launches_so_far();
+
+}  // namespace cutc

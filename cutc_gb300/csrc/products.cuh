@@ -1,0 +1,21 @@
+// Pair-product, expansion and assembly kernels: launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cutc {
+
+// out[tri(a,b) * ld + g] = w[g] chi_a(g) chi_b(g); chi[a * ld_chi + g]
+int launch_sym_products(cudaStream_t st, int n, int nA, const double *w, const double *chi,
+                        int64_t ld_chi, double *out, int64_t ld);
+// out[stri(c,d) * ld + m n + g] = w (chi_c d_m chi_d - chi_d d_m chi_c), c > d
+int launch_antisym_products(cudaStream_t st, int n, int nA, const double *w, const double *aos,
+                            double *out, int64_t ld);
+// full AO-pair rows from packed rows
+int launch_expand_pairs(cudaStream_t st, int64_t rows, int nA, const double *Xp, int64_t ldp,
+                        double *X);
+// int_2e = A + A^T from the packed symmetric (H) and antisymmetric (N) parts
+int launch_assemble_int2e(cudaStream_t st, int nA, const double *H, const double *N, double *out);
+
+}  // namespace cutc

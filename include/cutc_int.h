@@ -1,0 +1,127 @@
+/*
+ * cutc_int.h -- C-ABI of the GB300 transcorrelated-integral engine
+ * (libcutcint.so, built for sm_103a).
+ *
+ * Drop-in surface: `cutc_int` keeps the argument list, array layouts and
+ * return codes of CuTC's entry point (src/cutc_int.c:15-20, declared for
+ * Fortran in src/cutc_module.f90:10-39).  Everything else in this header is an
+ * extension with plain pointers and sizes only.
+ *
+ * Array layouts (Fortran column-major, FP64 unless noted):
+ *   r1(3, n_grid1)   wr1(n_grid1)   r2(3, n_grid2)   wr2(n_grid2)   rn(3, n_nuc)
+ *   aos_data1(n_grid1, n_ao, 4)     aos_data2(n_grid2, n_ao, 4)   [value, d/dx, d/dy, d/dz]
+ *   c_bh(size_bh, n_nuc)   m_bh, n_bh, o_bh(size_bh, n_nuc) int32, exponents in [0, 6]
+ * Outputs:
+ *   int2_grad1_u12_ao(n_ao, n_ao, n_grid1, 3)   X_{mu nu}(r1) = sum_r2 w2 chi_mu chi_nu grad1 u
+ *   int_2e_ao(n_ao, n_ao, n_ao, n_ao)           two-electron TC integrals (A + A^T)
+ */
+#ifndef CUTC_GB300_CUTC_INT_H
+#define CUTC_GB300_CUTC_INT_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define CUTC_OK 0
+#define CUTC_ERR_LAUNCH_DIMS (-1) /* same code and condition as src/cutc_int.c:79-86 */
+#define CUTC_ERR_INVALID (-2)     /* bad size, NULL pointer, exponent outside [0, 6] */
+#define CUTC_ERR_NO_MEMORY (-3)   /* device memory exhausted even after tiling */
+#define CUTC_ERR_CUDA (-4)        /* CUDA / cuBLAS failure (message in cutc_last_error) */
+#define CUTC_ERR_NO_DEVICE (-5)   /* no usable sm_103 GPU */
+#define CUTC_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up */
+
+/* ---- precision forms --------------------------------------------------- */
+#define CUTC_PLAIN_FP64 0 /* FP64 contractions: the drop-in form */
+#define CUTC_SPLIT_BF16 1 /* FP64 operands split into BF16 slices on tcgen05, FP64 recombination */
+
+/*
+ * Drop-in replacement for CuTC's cutc_int (src/cutc_int.c:15-20).
+ * All pointers are host pointers (pageable is fine).  The six launch integers
+ * are validated exactly as the reference does (block volume against the
+ * device's maxThreadsPerBlock, grid against maxGridSize; -1 on failure) and
+ * are otherwise ignored: the engine picks its own launch geometry.
+ * Only the first three components of X are written, as in the reference
+ * (src/cutc_int.c:105,210).  Computes in the plain FP64 form.
+ * Returns CUTC_OK or a negative status; never calls exit().
+ */
+int cutc_int(int nxBlocks, int nyBlocks, int nzBlocks,
+             int blockxSize, int blockySize, int blockzSize,
+             int n_grid1, int n_grid2, int n_ao, int n_nuc, int size_bh,
+             double *r1, double *wr1, double *r2, double *wr2, double *rn,
+             double *aos_data1, double *aos_data2,
+             double *c_bh, int *m_bh, int *n_bh, int *o_bh,
+             double *int2_grad1_u12_ao, double *int_2e_ao);
+
+/* ---- extended API (no reference counterpart) --------------------------- */
+typedef struct cutc_options {
+    int precision;          /* CUTC_PLAIN_FP64 or CUTC_SPLIT_BF16 */
+    int n_slices;           /* split form: BF16 slices per operand, 3..7 (default 5) */
+    double a_en;            /* e-n Jastrow scale: f = a r / (1 + a r); 1.0 = reference */
+    double a_ee;            /* e-e Jastrow scale; 1.0 = reference */
+    int x_components;       /* X components copied out: 3 (reference) or 4 */
+    int device_pointers;    /* 1: every array argument is a device pointer */
+    size_t max_work_bytes;  /* device budget for the r1 tiles; 0 = automatic */
+    void *stream;           /* cudaStream_t to run on; NULL = the engine's stream */
+} cutc_options;
+
+typedef struct cutc_stats {
+    double ms_total;        /* wall time of the call */
+    double ms_h2d;          /* host -> device copies */
+    double ms_pair;         /* pair terms (grad1 u) */
+    double ms_x;            /* X contraction(s) incl. slicing */
+    double ms_int2e;        /* int_2e contraction(s) + assembly */
+    double ms_d2h;          /* device -> host copies */
+    int n_r1_tiles;         /* r1 tiles the X build was split into */
+    int gpu_launches;       /* kernels of this library launched by the call */
+} cutc_stats;
+
+/* Fills the defaults: plain FP64, 5 slices, a_en = a_ee = 1, 3 X components. */
+void cutc_default_options(cutc_options *opt);
+
+/*
+ * cutc_int with options.  With opt->device_pointers = 1 all array arguments
+ * (inputs and outputs) are device pointers on the current device and no
+ * host<->device copies are made.  stats may be NULL.
+ */
+int cutc_int_ex(const cutc_options *opt,
+                int n_grid1, int n_grid2, int n_ao, int n_nuc, int size_bh,
+                const double *r1, const double *wr1, const double *r2, const double *wr2,
+                const double *rn, const double *aos_data1, const double *aos_data2,
+                const double *c_bh, const int *m_bh, const int *n_bh, const int *o_bh,
+                double *int2_grad1_u12_ao, double *int_2e_ao, cutc_stats *stats);
+
+/*
+ * Pair terms alone, on device pointers: for r1 rows [i0, i0 + n1b) and all
+ * r2 points, writes grad1u[c * n1b * n2 + i * n2 + j] for c = 0..2 (gradient)
+ * and c = 3 (-1/2 |grad1 u|^2): the layout of grad1_u12 in the reference's
+ * cutc_int_bh (src/jast_bh.cu:268-303), without its launch-geometry
+ * arguments.  Synchronous on the engine stream.
+ */
+int cutc_jast_bh_dev(int i0, int n1b, int n_grid1, int n_grid2, int n_nuc, int size_bh,
+                     const double *r1, const double *r2, const double *rn,
+                     const double *c_bh, const int *m_bh, const int *n_bh, const int *o_bh,
+                     double a_en, double a_ee, double *grad1u);
+
+/*
+ * The launch-geometry check of src/cutc_int.c:79-86 against the current
+ * device: block volume > maxThreadsPerBlock or any grid extent > maxGridSize
+ * (unsigned comparisons, as the reference's dim3 arithmetic) returns
+ * CUTC_ERR_LAUNCH_DIMS (-1).
+ */
+int cutc_validate_launch_dims(int nxBlocks, int nyBlocks, int nzBlocks,
+                              int blockxSize, int blockySize, int blockzSize);
+
+/* Message describing the last non-zero status returned on this thread. */
+const char *cutc_last_error(void);
+
+/* Frees the engine's cached device workspace on the current device. */
+void cutc_release(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

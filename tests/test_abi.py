@@ -1,0 +1,51 @@
+"""The C-ABI library builds, loads without a GPU and exports what the header declares."""
+import os
+import re
+
+import pytest
+
+import cutc_gb300 as cg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fn)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(cutc_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_the_drop_in_signature():
+    names = declared_functions()
+    assert "cutc_int" in names
+    text = open(os.path.join(ROOT, "include", "cutc_int.h")).read()
+    # the argument list of src/cutc_int.c:15-20
+    sig = re.search(r"int cutc_int\((.*?)\);", text, flags=re.S).group(1)
+    params = [p.strip().split()[-1].lstrip("*") for p in sig.split(",")]
+    assert params == ["nxBlocks", "nyBlocks", "nzBlocks", "blockxSize", "blockySize",
+                      "blockzSize", "n_grid1", "n_grid2", "n_ao", "n_nuc", "size_bh",
+                      "r1", "wr1", "r2", "wr2", "rn", "aos_data1", "aos_data2",
+                      "c_bh", "m_bh", "n_bh", "o_bh", "int2_grad1_u12_ao", "int_2e_ao"]
+
+
+def test_library_exports_every_declared_symbol():
+    L = cg.load()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+    assert sorted(declared_functions()) == sorted(cg.EXPORTS)
+
+
+def test_no_device_is_a_status_not_an_exit():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import numpy as np
+    z = np.zeros(16)
+    zi = np.zeros(16, dtype=np.int32)
+    s = cg.cutc_int(1, 1, 1, 32, 1, 1, 2, 2, 1, 1, 1, z, z, z, z, z, z, z, z, zi, zi, zi, z, z)
+    assert s == cg.CUTC_ERR_NO_DEVICE
+    assert "device" in cg.last_error()
