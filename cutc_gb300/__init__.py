@@ -30,7 +30,7 @@ SPLIT_BF16 = 1
 
 # every symbol include/cutc_int.h declares
 EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_default_options", "cutc_jast_bh_dev",
-           "cutc_validate_launch_dims", "cutc_last_error", "cutc_release"]
+           "cutc_split_gemm_dev", "cutc_validate_launch_dims", "cutc_last_error", "cutc_release"]
 
 
 class Options(ctypes.Structure):
@@ -77,6 +77,8 @@ def load(path: str = LIB_PATH):
     L.cutc_default_options.restype = None
     L.cutc_jast_bh_dev.argtypes = [i] * 6 + [vp] * 7 + [dp, dp, vp]
     L.cutc_jast_bh_dev.restype = i
+    L.cutc_split_gemm_dev.argtypes = [i, i, i, ctypes.c_longlong, vp, vp, vp, ctypes.c_longlong]
+    L.cutc_split_gemm_dev.restype = i
     L.cutc_validate_launch_dims.argtypes = [i] * 6
     L.cutc_validate_launch_dims.restype = i
     L.cutc_last_error.argtypes = []
@@ -162,3 +164,16 @@ def jast_bh_device(r1, r2, rn, c_bh, m_bh, n_bh, o_bh, G, i0=0, n1b=None,
     return L.cutc_jast_bh_dev(i0, n1b, n1, r2.shape[0], rn.shape[0], c_bh.shape[1],
                               _vp(r1), _vp(r2), _vp(rn), _vp(c_bh), _vp(m_bh), _vp(n_bh),
                               _vp(o_bh), a_en, a_ee, _vp(G))
+
+
+def split_gemm_device(A, B, C=None, n_slices=5):
+    """C = A @ B.T through the split form, on device tensors (float64, row-major)."""
+    import torch
+    M, K = A.shape
+    N = B.shape[0]
+    if C is None:
+        C = torch.empty((N, M), dtype=torch.float64, device=A.device)  # column-major M x N
+    s = load().cutc_split_gemm_dev(n_slices, M, N, K, _vp(A), _vp(B), _vp(C), M)
+    if s != CUTC_OK:
+        raise CutcError(s, last_error())
+    return C.T

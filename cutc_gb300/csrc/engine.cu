@@ -564,6 +564,20 @@ extern "C" int cutc_jast_bh_dev(int i0, int n1b, int n_grid1, int n_grid2, int n
                          n_bh, o_bh, a_en, a_ee, grad1u);
 }
 
+extern "C" int cutc_split_gemm_dev(int n_slices, int M, int N, long long K, const double *A,
+                                   const double *B, double *C, long long ldc)
+{
+    if (M <= 0 || N <= 0 || K <= 0 || !A || !B || !C || ldc < M || n_slices < 3 ||
+        n_slices > kMaxSlices) {
+        cutc_set_error(CUTC_ERR_INVALID, "invalid split GEMM arguments");
+        return CUTC_ERR_INVALID;
+    }
+    Engine *E = nullptr;
+    CUTC_TRY(get_engine(&E));
+    std::lock_guard<std::mutex> lk(E->mu);
+    return split_gemm_dense(E, E->stream, n_slices, M, N, K, A, B, C, ldc);
+}
+
 extern "C" int cutc_validate_launch_dims(int gx, int gy, int gz, int bx, int by, int bz)
 {
     Engine *E = nullptr;

@@ -1,33 +1,826 @@
-// Split-precision (BF16-slice) contractions on tcgen05.
+// Split-precision contractions on the sm_103a tensor cores (tcgen05 + TMA).
+//
+// Both dense contractions of the cutc_int path
+//   X_m[p, r1] = sum_r2 P[p, r2] G_m[r1, r2]                    (X build)
+//   H[p, q] = sum_r1 X_3[p, r1] S0[q, r1],
+//   N[p, l] = -1/2 sum_{m, r1} X_m[p, r1] S_m[l, r1]          (int_2e)
+// are C[M x N] = alpha * A[M x K] B[N x K]^T with FP64 operands.  Each FP64
+// operand row r is written as
+//     A[r, k] = 2^{e_r} sum_{s < S} a_s[r, k],  a_s = q_s 2^{-8-9s},  q_s in [-256, 256]
+// (S signed 9-bit digits of the row-scaled value, rounded at the last digit:
+// relative error <= 2^{-9S}), and every digit is an exact BF16 number.  The
+// products a_s b_t with s + t <= S - 1 run as tcgen05.mma kind::f16 (BF16 in,
+// FP32 accumulate in tensor memory), one accumulator per diagonal d = s + t:
+//   * every product of diagonal d is an integer multiple of 2^{-16-9d} of
+//     magnitude <= 2^{-9d}, so the FP32 accumulator holds the exact sum while
+//     (d + 1) * Kc * 2^16 < 2^24; with the chunk Kc = 64 this holds for d <= 2;
+//   * after each chunk the d = 0 and d = 1 sums are added error-free into
+//     FP32 (hi, lo) register pairs (hi on a coarse grid, lo the remainder),
+//     d = 2 is added into an FP32 running sum kept in tensor memory, and the
+//     small diagonals d >= 3 stay in one tensor-memory accumulator for the
+//     whole K range;
+//   * the accumulators are double-buffered in tensor memory, so the flush of
+//     chunk c overlaps the MMAs of chunk c + 1;
+//   * at the end the pieces are summed in FP64 and scaled by alpha 2^{e_r + f_n}.
+// FP64 arithmetic is used only in that final recombination (and in the pair
+// terms that feed G), which is where GB300's scarce FP64 rate is affordable.
+// The scheme is the error-free splitting of Ozaki, Ogita, Oishi & Rump
+// (2012), on BF16 instead of FP64 slices, with exact FP32 chunk accumulation.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
 #include "common.cuh"
+#include "products.cuh"
 #include "split.cuh"
+#include "tc.cuh"
 
 namespace cutc {
 
-size_t split_r1_row_bytes(const Request &) { return 0; }
+// ---------------------------------------------------------------------------
+// GEMM kernel
+// ---------------------------------------------------------------------------
 
-static int not_built()
+constexpr int kBM = 128;        // rows of A per CTA (TMEM lanes)
+constexpr int kBN = 64;         // rows of B (output columns) per CTA
+constexpr int kBK = 32;         // K per TMA box: 32 BF16 = 64-byte rows (64B swizzle)
+constexpr int kChunkBlocks = 2; // exact-accumulation chunk: 64 K
+constexpr int kEpiWarps = 16;   // 4 lane quarters x 4 column groups of 16
+constexpr int kTmaWarp = kEpiWarps;
+constexpr int kMmaWarp = kEpiWarps + 1;
+constexpr int kGemmThreads = (kEpiWarps + 2) * 32;
+constexpr int kMaxKPerLaunch = 1 << 18;  // keeps every exact (hi, lo) sum below 2^24 units
+constexpr uint32_t kTmemCols = 512;
+// tensor-memory columns: buffer b holds diagonals 0, 1, 2 at 192 b + 64 d; d >= 3 at 384;
+// the epilogue keeps its running FP32 sum of diagonal 2 at 448
+constexpr uint32_t kAcc3Col = 384;
+constexpr uint32_t kSum2Col = 448;
+
+struct GemmParams {
+    int M, N;
+    int Mpad, Npad;
+    int kb0, nkb;          // K blocks [kb0, kb0 + nkb) of this launch
+    const int *ea;         // row exponents of A (Mpad)
+    const int *eb;         // row exponents of B (Npad)
+    double alpha;
+    double *C;
+    int64_t ldc;           // C[m + ldc * col(n)]
+    int ncol_group;        // col(n) = (n / ncol_group) * group_stride + col0 + n % ncol_group
+    int64_t group_stride;
+    int64_t col0;
+    int accumulate;        // C += result
+    int *err;              // set to a non-zero code if a bounded wait gave up
+};
+
+template <int S>
+struct GemmCfg {
+    static constexpr int kASlice = kBM * kBK * 2;
+    static constexpr int kBSlice = kBN * kBK * 2;
+    static constexpr int kStage = S * (kASlice + kBSlice);
+    static constexpr int kStages = (200 * 1024) / kStage < 4 ? (200 * 1024) / kStage : 4;
+    static constexpr int kBarBytes = 256;
+    static constexpr int kSmem = kStages * kStage + 1024 + kBarBytes;
+    static_assert(kStages >= 2, "not enough shared memory for two stages");
+};
+
+__device__ __forceinline__ double pow2(int e)
 {
-    cutc_set_error(CUTC_ERR_INVALID, "the split-precision form is not available in this build");
-    return CUTC_ERR_INVALID;
+    e = e < -1022 ? -1022 : (e > 1023 ? 1023 : e);
+    return __longlong_as_double((long long)(1023 + e) << 52);
 }
 
-int split_prepare_x(Engine *, const Request &, cudaStream_t, const double *, const double *,
-                    int64_t, int, SplitPlan &)
+template <int S>
+__global__ void __launch_bounds__(kGemmThreads, 1)
+split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  GemmParams P)
 {
-    return not_built();
+    using Cfg = GemmCfg<S>;
+    constexpr int D = S - 1;  // highest diagonal kept
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + Cfg::kStages * Cfg::kStage);
+    uint64_t *full = bars;
+    uint64_t *empty = bars + Cfg::kStages;
+    uint64_t *tfull = bars + 2 * Cfg::kStages;
+    uint64_t *tempty = tfull + 2;
+    uint64_t *drain = tempty + 2;
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(drain + 1);
+    volatile int *s_abort = reinterpret_cast<volatile int *>(s_tmem + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+    const int nkb = P.nkb;
+    const int nch = (nkb + kChunkBlocks - 1) / kChunkBlocks;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < Cfg::kStages; i++) {
+            tc::mbar_init(tc::smem_u32(&full[i]), 1);
+            tc::mbar_init(tc::smem_u32(&empty[i]), 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            tc::mbar_init(tc::smem_u32(&tfull[i]), 1);
+            tc::mbar_init(tc::smem_u32(&tempty[i]), kEpiWarps);
+        }
+        tc::mbar_init(tc::smem_u32(drain), 1);
+        *s_abort = 0;
+        tc::fence_mbar_init();
+    }
+    if (warp == kMmaWarp) {
+        tc::tmem_alloc(tc::smem_u32(s_tmem), kTmemCols);
+        tc::tmem_relinquish();
+    }
+    if (warp == kTmaWarp && lane == 0) {
+        tc::tma_prefetch(&tmA);
+        tc::tma_prefetch(&tmB);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *s_tmem;
+
+    auto fail = [&](int code) {
+        *s_abort = 1;
+        atomicExch(P.err, code);
+    };
+
+    if (warp == kTmaWarp) {
+        if (lane == 0) {
+            int issued = 0;
+            for (int kb = 0; kb < nkb; kb++) {
+                const int stage = kb % Cfg::kStages, round = kb / Cfg::kStages;
+                if (round > 0 &&
+                    !tc::mbar_wait(tc::smem_u32(&empty[stage]), (round - 1) & 1, s_abort)) {
+                    fail(1);
+                    break;
+                }
+                const uint32_t fb = tc::smem_u32(&full[stage]);
+                tc::mbar_arrive_expect_tx(fb, Cfg::kStage);
+                uint8_t *st = smem + stage * Cfg::kStage;
+                const int x = (P.kb0 + kb) * kBK;
+#pragma unroll
+                for (int s = 0; s < S; s++)
+                    tc::tma_load_2d(tc::smem_u32(st + s * Cfg::kASlice), &tmA, x, s * P.Mpad + m0, fb);
+#pragma unroll
+                for (int t = 0; t < S; t++)
+                    tc::tma_load_2d(tc::smem_u32(st + S * Cfg::kASlice + t * Cfg::kBSlice), &tmB, x,
+                                    t * P.Npad + n0, fb);
+                issued = kb + 1;
+            }
+            if (*s_abort) {
+                // let the copies already issued land before the CTA goes away
+                for (int kb = max(0, issued - Cfg::kStages); kb < issued; kb++)
+                    tc::mbar_wait(tc::smem_u32(&full[kb % Cfg::kStages]),
+                                  (kb / Cfg::kStages) & 1, nullptr);
+            }
+        }
+    } else if (warp == kMmaWarp) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
+            bool acc3_init = false;
+            bool ok = true;
+            for (int c = 0; c < nch && ok; c++) {
+                const int b = c & 1;
+                if (c >= 2 && !tc::mbar_wait(tc::smem_u32(&tempty[b]), ((c >> 1) - 1) & 1, s_abort)) {
+                    fail(2);
+                    break;
+                }
+                tc::fence_after_sync();
+                bool init[3] = {false, false, false};
+                const int kb_end = min(nkb, (c + 1) * kChunkBlocks);
+                for (int kb = c * kChunkBlocks; kb < kb_end; kb++) {
+                    const int stage = kb % Cfg::kStages, round = kb / Cfg::kStages;
+                    if (!tc::mbar_wait(tc::smem_u32(&full[stage]), round & 1, s_abort)) {
+                        fail(3);
+                        ok = false;
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    const uint32_t sa = tc::smem_u32(smem + stage * Cfg::kStage);
+                    const uint32_t sb = sa + S * Cfg::kASlice;
+#pragma unroll
+                    for (int s = 0; s < S; s++) {
+#pragma unroll
+                        for (int t = 0; t + s <= D; t++) {
+                            const int d = s + t;
+                            const uint32_t col = d < 3 ? 192u * b + 64u * d : kAcc3Col;
+#pragma unroll
+                            for (int k16 = 0; k16 < kBK / 16; k16++) {
+                                const uint64_t ad = tc::smem_desc_sw64(sa + s * Cfg::kASlice + k16 * 32);
+                                const uint64_t bd = tc::smem_desc_sw64(sb + t * Cfg::kBSlice + k16 * 32);
+                                uint32_t acc;
+                                if (d < 3) {
+                                    acc = init[d] ? 1u : 0u;
+                                    init[d] = true;
+                                } else {
+                                    acc = acc3_init ? 1u : 0u;
+                                    acc3_init = true;
+                                }
+                                tc::mma_bf16(tbase + col, ad, bd, idesc, acc);
+                            }
+                        }
+                    }
+                    tc::mma_commit(tc::smem_u32(&empty[stage]));
+                }
+                if (ok)
+                    tc::mma_commit(tc::smem_u32(&tfull[b]));
+            }
+            // all MMAs of this CTA have completed once the drain barrier flips
+            tc::mma_commit(tc::smem_u32(drain));
+            if (!tc::mbar_wait(tc::smem_u32(drain), 0, nullptr))
+                fail(5);
+        }
+    } else {
+        // ---- epilogue: exact chunk flushes, then FP64 recombination ----------
+        const int q = warp & 3, cgrp = warp >> 2;
+        const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        const uint32_t coff = 16u * cgrp;
+        float hi0[16], lo0[16], hi1[16], lo1[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+            hi0[j] = lo0[j] = hi1[j] = lo1[j] = 0.f;
+        const float C0 = 786432.0f;  // 1.5 * 2^19: rounds to multiples of 2^-4
+        const float C1 = 1536.0f;    // 1.5 * 2^10: rounds to multiples of 2^-13
+        bool ok = true;
+        for (int c = 0; c < nch; c++) {
+            const int b = c & 1;
+            if (!tc::mbar_wait(tc::smem_u32(&tfull[b]), (c >> 1) & 1, s_abort)) {
+                fail(4);
+                ok = false;
+                break;
+            }
+            tc::fence_after_sync();
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                float v[8];
+                const uint32_t cb = tbase + lane_off + 192u * b + coff + 8u * h;
+                tc::tmem_ld8(cb, v);
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const float x = v[j];
+                    const float hh = __fsub_rn(__fadd_rn(x, C0), C0);
+                    hi0[8 * h + j] = __fadd_rn(hi0[8 * h + j], hh);
+                    lo0[8 * h + j] = __fadd_rn(lo0[8 * h + j], __fsub_rn(x, hh));
+                }
+                tc::tmem_ld8(cb + 64u, v);
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const float x = v[j];
+                    const float hh = __fsub_rn(__fadd_rn(x, C1), C1);
+                    hi1[8 * h + j] = __fadd_rn(hi1[8 * h + j], hh);
+                    lo1[8 * h + j] = __fadd_rn(lo1[8 * h + j], __fsub_rn(x, hh));
+                }
+                if (D >= 2) {
+                    const uint32_t sum2 = tbase + lane_off + kSum2Col + coff + 8u * h;
+                    tc::tmem_ld8(cb + 128u, v);
+                    if (c > 0) {
+                        float a2[8];
+                        tc::tmem_ld8(sum2, a2);
+#pragma unroll
+                        for (int j = 0; j < 8; j++)
+                            v[j] = __fadd_rn(a2[j], v[j]);
+                    }
+                    tc::tmem_st8(sum2, v);
+                }
+            }
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0)
+                tc::mbar_arrive(tc::smem_u32(&tempty[b]));
+        }
+        const int m = m0 + q * 32 + lane;
+        const int em = (ok && m < P.M) ? P.ea[m] : 0;
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            float v3[4], a2[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                v3[j] = a2[j] = 0.f;
+            if (ok && D >= 3)
+                tc::tmem_ld4(tbase + lane_off + kAcc3Col + coff + 4u * h, v3);
+            if (ok && D >= 2 && nch > 0)
+                tc::tmem_ld4(tbase + lane_off + kSum2Col + coff + 4u * h, a2);
+            if (ok && m < P.M) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int jj = 4 * h + j;
+                    const int n = n0 + (int)coff + jj;
+                    if (n < P.N) {
+                        double val = ((double)hi0[jj] + (double)hi1[jj]) +
+                                     (((double)lo0[jj] + (double)lo1[jj]) +
+                                      ((double)a2[j] + (double)v3[j]));
+                        val *= P.alpha * pow2(em + P.eb[n]);
+                        const int64_t col = (int64_t)(n / P.ncol_group) * P.group_stride +
+                                            P.col0 + n % P.ncol_group;
+                        double *dst = P.C + m + P.ldc * col;
+                        *dst = P.accumulate ? *dst + val : val;
+                    }
+                }
+            }
+        }
+    }
+
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == kMmaWarp)
+        tc::tmem_dealloc(tbase, kTmemCols);
 }
 
-int split_x_tile(Engine *, const Request &, cudaStream_t, SplitPlan &, const double *, int, int,
-                 double *)
+// ---------------------------------------------------------------------------
+// slicing kernels
+// ---------------------------------------------------------------------------
+
+// Operand sources: value of row r, column k of an FP64 matrix.
+struct SrcDense {  // X[r * ld + k]
+    const double *X;
+    int64_t ld;
+    __device__ double operator()(int64_t r, int64_t k) const { return X[r * ld + k]; }
+};
+
+struct SrcSym {  // w[k] chi_a(k) chi_b(k), (a, b) = pairs[r]
+    const double *w, *chi;
+    int64_t ldchi;
+    const int2 *pairs;
+    __device__ double operator()(int64_t r, int64_t k) const
+    {
+        const int2 ab = pairs[r];
+        const double wa = w[k] * chi[ab.x * ldchi + k];
+        return wa * chi[ab.y * ldchi + k];
+    }
+};
+
+struct SrcAnti {  // w (chi_c d_m chi_d - chi_d d_m chi_c), k = m n + g, (c, d) = pairs[r]
+    const double *w, *aos;
+    int n, nA;
+    const int2 *pairs;
+    __device__ double operator()(int64_t r, int64_t k) const
+    {
+        const int m = (int)(k / n), g = (int)(k % n);
+        const int2 cd = pairs[r];
+        const int64_t comp = (int64_t)nA * n * (m + 1);
+        const double vc = aos[(int64_t)cd.x * n + g], vd = aos[(int64_t)cd.y * n + g];
+        return w[g] * (vc * aos[comp + (int64_t)cd.y * n + g] - vd * aos[comp + (int64_t)cd.x * n + g]);
+    }
+};
+
+__device__ __forceinline__ void atomic_max_abs(unsigned long long *dst, double v)
 {
-    return not_built();
+    atomicMax(dst, (unsigned long long)__double_as_longlong(fabs(v)));
 }
 
-int split_int2e(Engine *, const Request &, cudaStream_t, SplitPlan &, const double *,
-                const double *, const double *, double *)
+// rmax[r] = bits of max_k |src(r, k)| (non-negative doubles order like their bits)
+template <class Src>
+__global__ void rowmax_kernel(Src src, int rows, int64_t K, int64_t kper,
+                              unsigned long long *rmax)
 {
-    return not_built();
+    const int r = blockIdx.x;
+    if (r >= rows)
+        return;
+    const int64_t k0 = (int64_t)blockIdx.y * kper;
+    const int64_t k1 = min(K, k0 + kper);
+    double m = 0.0;
+    for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x)
+        m = fmax(m, fabs(src(r, k)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0 && m > 0.0)
+            atomic_max_abs(&rmax[r], m);
+    }
+}
+
+// Row maxima of a matrix stored column by column: src[(k0 + k) * ld + r].
+__global__ void rowmax_cols_kernel(const double *X, int64_t ld, int64_t k0, int rows, int64_t K,
+                                   int64_t kper, unsigned long long *rmax)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows)
+        return;
+    const int64_t ka = (int64_t)blockIdx.y * kper, kb = min(K, ka + kper);
+    double m = 0.0;
+    for (int64_t k = ka; k < kb; k++)
+        m = fmax(m, fabs(X[(k0 + k) * ld + r]));
+    if (m > 0.0)
+        atomic_max_abs(&rmax[r], m);
+}
+
+// Exponent e with |x| < 2^e for every x of the row; 0 for zero (or denormal-only) rows.
+__device__ __forceinline__ int row_exponent(unsigned long long bits)
+{
+    const int E = (int)((bits >> 52) & 0x7ff);
+    return E == 0 ? 0 : E - 1022;
+}
+
+// The S signed base-2^9 digits of x 2^{-e} (first digit scaled by 2^8),
+// computed in 64-bit integer arithmetic and returned as exact BF16 values
+// q_s 2^{-8-9s}.
+template <int S>
+__device__ __forceinline__ void split_digits(double x, int e, __nv_bfloat16 (&out)[S])
+{
+    constexpr int F = 8 + 9 * (S - 1);
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((bits >> 52) & 0x7ff);
+    long long t = 0;
+    if (E != 0) {
+        const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+        const int sh = E - 1075 - e + F;
+        unsigned long long T;
+        if (sh >= 0)
+            T = mant << sh;  // < 2^F because |x| < 2^e
+        else if (sh > -64)
+            T = (mant + (1ull << (-sh - 1))) >> (-sh);
+        else
+            T = 0;
+        t = (bits >> 63) ? -(long long)T : (long long)T;
+    }
+    int q[S];
+#pragma unroll
+    for (int s = S - 1; s >= 1; s--) {
+        const long long d = ((t + 256) & 511) - 256;
+        q[s] = (int)d;
+        t = (t - d) >> 9;
+    }
+    q[0] = (int)t;
+#pragma unroll
+    for (int s = 0; s < S; s++)
+        out[s] = __float2bfloat16_rn(__int2float_rn(q[s]) * exp2f((float)(-8 - 9 * s)));
+}
+
+// slices[(s * Mpad + r) * Kpad + k] for r < Mpad, k < Kpad (zeros outside M x K);
+// ex[r] = row exponent.
+template <int S, class Src>
+__global__ void slice_kernel(Src src, int M, int64_t K, int64_t Kpad, int Mpad,
+                             const unsigned long long *rmax, __nv_bfloat16 *slices, int *ex)
+{
+    const int r = blockIdx.y;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= Kpad)
+        return;
+    const int e = r < M ? row_exponent(rmax[r]) : 0;
+    if (k == 0)
+        ex[r] = e;
+    __nv_bfloat16 d[S];
+    const double x = (r < M && k < K) ? src(r, k) : 0.0;
+    split_digits<S>(x, e, d);
+#pragma unroll
+    for (int s = 0; s < S; s++)
+        slices[((int64_t)s * Mpad + r) * Kpad + k] = d[s];
+}
+
+// Same for a matrix stored column by column, src[(k0 + k) * ld + r], through a
+// 32 x 32 shared-memory transpose so reads and writes are both coalesced.
+template <int S>
+__global__ void slice_cols_kernel(const double *X, int64_t ld, int64_t k0, int M, int64_t K,
+                                  int64_t Kpad, int Mpad, const unsigned long long *rmax,
+                                  __nv_bfloat16 *slices, int *ex)
+{
+    __shared__ double tile[32][33];
+    const int r0 = blockIdx.y * 32;
+    const int64_t kb = (int64_t)blockIdx.x * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int i = ty; i < 32; i += blockDim.y) {
+        const int64_t k = kb + i;
+        const int r = r0 + tx;
+        tile[i][tx] = (r < M && k < K) ? X[(k0 + k) * ld + r] : 0.0;
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += blockDim.y) {
+        const int r = r0 + i;
+        const int64_t k = kb + tx;
+        if (r >= Mpad || k >= Kpad)
+            continue;
+        const int e = r < M ? row_exponent(rmax[r]) : 0;
+        if (k == 0)
+            ex[r] = e;
+        __nv_bfloat16 d[S];
+        split_digits<S>(tile[tx][i], e, d);
+#pragma unroll
+        for (int s = 0; s < S; s++)
+            slices[((int64_t)s * Mpad + r) * Kpad + k] = d[s];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static int get_encode(EncodeTiledFn *fn)
+{
+    static EncodeTiledFn cached = nullptr;
+    if (!cached) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                         cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+            cudaGetLastError();
+            cutc_set_error(CUTC_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+            return CUTC_ERR_CUDA;
+        }
+        cached = (EncodeTiledFn)p;
+    }
+    *fn = cached;
+    return CUTC_OK;
+}
+
+// 2-D map over slices [rows_total][Kpad] BF16, box = kBK x box_rows, 64B swizzle.
+static int make_tmap(CUtensorMap *map, const void *base, int64_t rows_total, int64_t Kpad,
+                     int box_rows)
+{
+    EncodeTiledFn enc;
+    CUTC_TRY(get_encode(&enc));
+    cuuint64_t dims[2] = {(cuuint64_t)Kpad, (cuuint64_t)rows_total};
+    cuuint64_t strides[1] = {(cuuint64_t)Kpad * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims,
+                     strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        cutc_set_error(CUTC_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return CUTC_ERR_CUDA;
+    }
+    return CUTC_OK;
+}
+
+
+static int alloc_operand(Workspace &W, int slot, int S, int M, int row_mult, int64_t K,
+                         Operand &op)
+{
+    op.M = M;
+    op.Mpad = (int)round_up(std::max(M, 1), row_mult);
+    op.K = K;
+    op.Kpad = round_up(std::max<int64_t>(K, 1), kBK);
+    void *p;
+    CUTC_TRY(W.get(slot, (size_t)S * op.Mpad * op.Kpad * 2, &p));
+    op.sl = p;
+    CUTC_TRY(W.get(slot + 1, (size_t)op.Mpad * 4, &p));
+    op.ex = (int *)p;
+    CUTC_TRY(W.get(slot + 2, (size_t)op.Mpad * 8, &p));
+    op.rmax = (unsigned long long *)p;
+    return CUTC_OK;
+}
+
+template <int S, class Src>
+static int slice_rows(cudaStream_t st, Src src, Operand &op)
+{
+    CUTC_CUDA_TRY(cudaMemsetAsync(op.rmax, 0, (size_t)op.Mpad * 8, st));
+    if (op.M > 0 && op.K > 0) {
+        const int64_t kper = 16384;
+        dim3 g1((unsigned)op.M, ceil_div(op.K, kper));
+        rowmax_kernel<Src><<<g1, 256, 0, st>>>(src, op.M, op.K, kper, op.rmax);
+        CUTC_CUDA_TRY(cudaGetLastError());
+    }
+    if (op.Mpad > 65535) {
+        cutc_set_error(CUTC_ERR_INVALID, "operand with %d rows exceeds the slicer grid", op.Mpad);
+        return CUTC_ERR_INVALID;
+    }
+    dim3 g2(ceil_div(op.Kpad, 256), (unsigned)op.Mpad);
+    slice_kernel<S, Src><<<g2, 256, 0, st>>>(src, op.M, op.K, op.Kpad, op.Mpad, op.rmax,
+                                             (__nv_bfloat16 *)op.sl, op.ex);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    note_launches(2);
+    return CUTC_OK;
+}
+
+template <int S>
+static int slice_cols(cudaStream_t st, const double *X, int64_t ld, int64_t k0, Operand &op)
+{
+    CUTC_CUDA_TRY(cudaMemsetAsync(op.rmax, 0, (size_t)op.Mpad * 8, st));
+    if (op.M > 0 && op.K > 0) {
+        const int64_t kper = 512;
+        dim3 g1(ceil_div(op.M, 128), ceil_div(op.K, kper));
+        rowmax_cols_kernel<<<g1, 128, 0, st>>>(X, ld, k0, op.M, op.K, kper, op.rmax);
+        CUTC_CUDA_TRY(cudaGetLastError());
+    }
+    dim3 g2(ceil_div(op.Kpad, 32), ceil_div(op.Mpad, 32));
+    slice_cols_kernel<S><<<g2, dim3(32, 8), 0, st>>>(X, ld, k0, op.M, op.K, op.Kpad, op.Mpad,
+                                                     op.rmax, (__nv_bfloat16 *)op.sl, op.ex);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    note_launches(2);
+    return CUTC_OK;
+}
+
+// C = alpha A B^T (+ C) over the operands' common K.
+template <int S>
+static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alpha, double *C,
+                int64_t ldc, int ncol_group, int64_t group_stride, int64_t col0, int accumulate,
+                int *err)
+{
+    using Cfg = GemmCfg<S>;
+    static bool attr = false;
+    if (!attr) {
+        CUTC_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<S>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem));
+        attr = true;
+    }
+    CUtensorMap ta, tb;
+    CUTC_TRY(make_tmap(&ta, A.sl, (int64_t)S * A.Mpad, A.Kpad, kBM));
+    CUTC_TRY(make_tmap(&tb, B.sl, (int64_t)S * B.Mpad, B.Kpad, kBN));
+    const int nkb_total = (int)(A.Kpad / kBK);
+    const int kb_per = kMaxKPerLaunch / kBK;
+    dim3 grid(A.Mpad / kBM, B.Mpad / kBN);
+    if (grid.y > 65535) {
+        cutc_set_error(CUTC_ERR_INVALID, "GEMM N extent too large (%d tiles)", (int)grid.y);
+        return CUTC_ERR_INVALID;
+    }
+    for (int kb0 = 0; kb0 < nkb_total; kb0 += kb_per) {
+        GemmParams P;
+        P.M = A.M;
+        P.N = B.M;
+        P.Mpad = A.Mpad;
+        P.Npad = B.Mpad;
+        P.kb0 = kb0;
+        P.nkb = std::min(kb_per, nkb_total - kb0);
+        P.ea = A.ex;
+        P.eb = B.ex;
+        P.alpha = alpha;
+        P.C = C;
+        P.ldc = ldc;
+        P.ncol_group = ncol_group;
+        P.group_stride = group_stride;
+        P.col0 = col0;
+        P.accumulate = (accumulate || kb0 > 0) ? 1 : 0;
+        P.err = err;
+        split_gemm_kernel<S><<<grid, kGemmThreads, Cfg::kSmem, st>>>(ta, tb, P);
+        CUTC_CUDA_TRY(cudaGetLastError());
+        note_launches(1);
+    }
+    return CUTC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the plan for one build
+// ---------------------------------------------------------------------------
+
+enum SplitSlot {
+    SS_PAIRS_SYM = 0, SS_PAIRS_ANTI = 1, SS_ERR = 2,
+    SS_AX = 3, SS_BX = 6, SS_AH = 9, SS_AN = 12, SS_BH = 15, SS_BN = 18, SS_H = 21, SS_N = 22,
+};
+
+
+size_t split_r1_row_bytes(const Request &R)
+{
+    // BF16 slices of the four G rows of one r1 point
+    return 4 * (size_t)R.n_slices * round_up(R.n2, kBK) * 2;
+}
+
+static int upload_pairs(Workspace &W, int slot, cudaStream_t st, int nA, bool strict, int2 **out)
+{
+    std::vector<int2> v;
+    for (int b = 0; b < nA; b++)
+        for (int a = strict ? b + 1 : b; a < nA; a++)
+            v.push_back(make_int2(a, b));  // packed order of tri_index / stri_index
+    void *p;
+    CUTC_TRY(W.get(slot, std::max<size_t>(1, v.size()) * sizeof(int2), &p));
+    if (!v.empty())
+        CUTC_CUDA_TRY(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    CUTC_CUDA_TRY(cudaStreamSynchronize(st));  // v goes out of scope
+    *out = (int2 *)p;
+    return CUTC_OK;
+}
+
+#define CUTC_SLICES_DISPATCH(S_, CALL)                                         \
+    switch (S_) {                                                              \
+    case 3: { constexpr int S = 3; CALL; } break;                              \
+    case 4: { constexpr int S = 4; CALL; } break;                              \
+    case 5: { constexpr int S = 5; CALL; } break;                              \
+    case 6: { constexpr int S = 6; CALL; } break;                              \
+    case 7: { constexpr int S = 7; CALL; } break;                              \
+    default:                                                                   \
+        cutc_set_error(CUTC_ERR_INVALID, "unsupported slice count %d", S_);    \
+        return CUTC_ERR_INVALID;                                               \
+    }
+
+int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *wr2,
+                    const double *aos2v, int64_t n1t, int slot0, SplitPlan &sp)
+{
+    Workspace &W = E->ws;
+    SplitPlan &S_ = sp;
+    sp.slot0 = slot0;
+    sp.n_slices = R.n_slices;
+    sp.n1t = n1t;
+    const int np = (int)n_pairs(R.nA);
+    void *p;
+    CUTC_TRY(W.get(slot0 + SS_ERR, 64, &p));
+    S_.err = (int *)p;
+    CUTC_CUDA_TRY(cudaMemsetAsync(S_.err, 0, 4, st));
+    CUTC_TRY(upload_pairs(W, slot0 + SS_PAIRS_SYM, st, R.nA, false, &S_.pairs_sym));
+    CUTC_TRY(upload_pairs(W, slot0 + SS_PAIRS_ANTI, st, R.nA, true, &S_.pairs_anti));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_AX, R.n_slices, np, kBM, R.n2, S_.AX));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BX, R.n_slices, (int)(4 * n1t), kBN, R.n2, S_.BX));
+    SrcSym src{wr2, aos2v, (int64_t)R.n2, S_.pairs_sym};
+    CUTC_SLICES_DISPATCH(R.n_slices, CUTC_TRY((slice_rows<S, SrcSym>(st, src, S_.AX))));
+    return CUTC_OK;
+}
+
+int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const double *G,
+                 int i0, int nb, double *Xp)
+{
+    (void)E;
+    SplitPlan &S_ = sp;
+    Operand B = S_.BX;
+    B.M = 4 * nb;  // rows (c, i) of this tile; Mpad keeps the allocated padding
+    B.Mpad = (int)round_up(B.M, kBN);
+    const int64_t np = n_pairs(R.nA);
+    SrcDense src{G, (int64_t)R.n2};
+    CUTC_SLICES_DISPATCH(sp.n_slices, {
+        CUTC_TRY((slice_rows<S, SrcDense>(st, src, B)));
+        CUTC_TRY((gemm<S>(st, S_.AX, B, 1.0, Xp, np, nb, R.n1, i0, 0, S_.err)));
+    });
+    return CUTC_OK;
+}
+
+int split_int2e(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const double *wr1,
+                const double *aos1, const double *Xp, double *I)
+{
+    Workspace &W = E->ws;
+    SplitPlan &S_ = sp;
+    const int slot0 = sp.slot0;
+    const int n1 = R.n1, nA = R.nA;
+    const int np = (int)n_pairs(nA), nl = (int)n_strict_pairs(nA);
+    Operand AH, AN, BH, BN;
+    CUTC_TRY(alloc_operand(W, slot0 + SS_AH, sp.n_slices, np, kBM, n1, AH));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_AN, sp.n_slices, np, kBM, 3 * (int64_t)n1, AN));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BH, sp.n_slices, np, kBN, n1, BH));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BN, sp.n_slices, std::max(nl, 1), kBN, 3 * (int64_t)n1, BN));
+    BN.M = nl;
+    void *p;
+    CUTC_TRY(W.get(slot0 + SS_H, (size_t)np * np * 8, &p));
+    double *H = (double *)p;
+    CUTC_TRY(W.get(slot0 + SS_N, (size_t)np * std::max(nl, 1) * 8, &p));
+    double *N = (double *)p;
+    SrcSym s0{wr1, aos1, (int64_t)n1, S_.pairs_sym};
+    SrcAnti sa{wr1, aos1, n1, nA, S_.pairs_anti};
+    CUTC_SLICES_DISPATCH(sp.n_slices, {
+        CUTC_TRY(slice_cols<S>(st, Xp, np, 3 * (int64_t)n1, AH));
+        CUTC_TRY(slice_cols<S>(st, Xp, np, 0, AN));
+        CUTC_TRY((slice_rows<S, SrcSym>(st, s0, BH)));
+        CUTC_TRY(gemm<S>(st, AH, BH, 1.0, H, np, np, 0, 0, 0, S_.err));
+        if (nl > 0) {
+            CUTC_TRY((slice_rows<S, SrcAnti>(st, sa, BN)));
+            CUTC_TRY(gemm<S>(st, AN, BN, -0.5, N, np, nl, 0, 0, 0, S_.err));
+        }
+    });
+    CUTC_TRY(launch_assemble_int2e(st, nA, H, N, I));
+    note_launches(1);
+    int herr = 0;
+    CUTC_CUDA_TRY(cudaMemcpyAsync(&herr, S_.err, 4, cudaMemcpyDeviceToHost, st));
+    CUTC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (herr) {
+        cutc_set_error(CUTC_ERR_TIMEOUT, "a tensor-core pipeline wait gave up (code %d)", herr);
+        return CUTC_ERR_TIMEOUT;
+    }
+    return CUTC_OK;
+}
+
+// Split-precision GEMM on device arrays: C[m + ldc n] = sum_k A[m K + k] B[n K + k].
+int split_gemm_dense(Engine *E, cudaStream_t st, int n_slices, int M, int N, int64_t K,
+                     const double *A, const double *B, double *C, int64_t ldc)
+{
+    Workspace &W = E->ws;
+    const int base = 200;
+    Operand OA, OB;
+    CUTC_TRY(alloc_operand(W, base, n_slices, M, kBM, K, OA));
+    CUTC_TRY(alloc_operand(W, base + 3, n_slices, N, kBN, K, OB));
+    void *p;
+    CUTC_TRY(W.get(base + 6, 64, &p));
+    int *err = (int *)p;
+    CUTC_CUDA_TRY(cudaMemsetAsync(err, 0, 4, st));
+    SrcDense sa{A, K}, sb{B, K};
+    CUTC_SLICES_DISPATCH(n_slices, {
+        CUTC_TRY((slice_rows<S, SrcDense>(st, sa, OA)));
+        CUTC_TRY((slice_rows<S, SrcDense>(st, sb, OB)));
+        CUTC_TRY(gemm<S>(st, OA, OB, 1.0, C, ldc, N, 0, 0, 0, err));
+    });
+    int herr = 0;
+    CUTC_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+    CUTC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (herr) {
+        cutc_set_error(CUTC_ERR_TIMEOUT, "a tensor-core pipeline wait gave up (code %d)", herr);
+        return CUTC_ERR_TIMEOUT;
+    }
+    return CUTC_OK;
 }
 
 }  // namespace cutc

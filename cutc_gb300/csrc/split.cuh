@@ -11,14 +11,24 @@ namespace cutc {
 constexpr int kMaxSlices = 7;
 constexpr int kDefaultSlices = 5;
 
+// One FP64 operand as S BF16 slices [S][Mpad][Kpad] plus row exponents.
+struct Operand {
+    void *sl = nullptr;               // __nv_bfloat16 slices
+    int *ex = nullptr;                // row exponents (Mpad)
+    unsigned long long *rmax = nullptr;
+    int M = 0, Mpad = 0;
+    int64_t K = 0, Kpad = 0;
+};
+
 struct SplitPlan {
     int slot0 = 0;
     int n_slices = 0;
     int64_t n1t = 0;
-    void *a_slices = nullptr;  // P slices (X-build A operand)
-    float *a_scale = nullptr;
-    void *b_slices = nullptr;  // G-tile slices (X-build B operand)
-    float *b_scale = nullptr;
+    Operand AX;                        // P slices: X-build A operand
+    Operand BX;                        // G-tile slices: X-build B operand
+    int2 *pairs_sym = nullptr;         // (a, b), a >= b, in tri_index order
+    int2 *pairs_anti = nullptr;        // (a, b), a > b, in stri_index order
+    int *err = nullptr;                // device flag set by a bounded wait that gave up
 };
 
 size_t split_r1_row_bytes(const Request &R);
@@ -28,5 +38,8 @@ int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, co
                  int i0, int nb, double *Xp);
 int split_int2e(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const double *wr1,
                 const double *aos1, const double *Xp, double *I);
+// C[m + ldc n] = sum_k A[m K + k] B[n K + k] through the split form (device arrays)
+int split_gemm_dense(Engine *E, cudaStream_t st, int n_slices, int M, int N, int64_t K,
+                     const double *A, const double *B, double *C, int64_t ldc);
 
 }  // namespace cutc

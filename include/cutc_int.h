@@ -106,6 +106,17 @@ int cutc_jast_bh_dev(int i0, int n1b, int n_grid1, int n_grid2, int n_nuc, int s
                      double a_en, double a_ee, double *grad1u);
 
 /*
+ * The split-precision contraction alone, on device arrays of the current
+ * device: C[m + ldc * n] = sum_k A[m * K + k] * B[n * K + k] for m < M, n < N,
+ * with A and B FP64 row-major (K contiguous) and the product formed from
+ * n_slices BF16 slices per operand on the tcgen05 tensor cores (3..7 slices).
+ * This is the kernel behind CUTC_SPLIT_BF16, exposed for callers that need the
+ * GEMM itself.  Synchronous on the engine stream.  No reference counterpart.
+ */
+int cutc_split_gemm_dev(int n_slices, int M, int N, long long K,
+                        const double *A, const double *B, double *C, long long ldc);
+
+/*
  * The launch-geometry check of src/cutc_int.c:79-86 against the current
  * device: block volume > maxThreadsPerBlock or any grid extent > maxGridSize
  * (unsigned comparisons, as the reference's dim3 arithmetic) returns

@@ -1,0 +1,81 @@
+"""The split-precision form (BF16 slices on tcgen05) of the whole build.
+
+Tolerance: 1e-10 relative (normwise and max-abs/max) against the FP64 oracle
+for X and int_2e at the default 5 slices -- the accuracy target of the split
+form.  The plain FP64 form is the drop-in; this form trades the last ~2
+decimal digits for tensor-core speed.
+"""
+import numpy as np
+import pytest
+
+import cutc_gb300 as cg
+from cutc_gb300 import synth
+from golden_util import CASE_NAMES, load_case
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL_SPLIT = 1e-10
+
+
+def _check(X, I, Xr, Ir, tol=TOL_SPLIT):
+    ex, ei = oracle.rel_err(X, Xr), oracle.rel_err(I, Ir)
+    assert ex["norm"] < tol and ex["max"] < tol, ex
+    assert ei["norm"] < tol and ei["max"] < tol, ei
+    return ex, ei
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_split_matches_reference_golden(name):
+    p, ref = load_case(name)
+    X, I = cg.build_integrals(p, cg.SPLIT_BF16)
+    _check(X, I, ref["X"], ref["int2e"])
+
+
+def test_split_small_workload_vs_oracle():
+    p = synth.make_config("small")
+    X, I = cg.build_integrals(p, cg.SPLIT_BF16)
+    Xo, Io = oracle.cutc_int(p)
+    _check(X, I, Xo, Io)
+
+
+def test_split_r1_tiling_is_exact():
+    p = synth.make_problem(n_nuc=3, n_ao=9, n_grid1=300, n_grid2=700, size_bh=6, seed=21)
+    X1, I1 = cg.build_integrals(p, cg.SPLIT_BF16)
+    X2, I2, st = cg.build_integrals(p, cg.SPLIT_BF16, max_work_bytes=2 << 20, with_stats=True)
+    assert st["n_r1_tiles"] > 1
+    # the slices of each G row do not depend on the tile; only the int_2e sum order can
+    assert np.array_equal(X1, X2)
+    assert oracle.rel_err(I2, I1)["max"] < 1e-13
+
+
+def test_split_four_components_and_scale_factors():
+    p = synth.make_problem(n_nuc=2, n_ao=7, n_grid1=150, n_grid2=500, size_bh=5, seed=9,
+                           a_en=1.3, a_ee=0.6)
+    X, I = cg.build_integrals(p, cg.SPLIT_BF16, x_components=4)
+    Xo, Io = oracle.cutc_int(p)
+    _check(X[:3], I, Xo, Io)
+
+
+def test_split_slice_count_controls_accuracy():
+    p = synth.make_problem(n_nuc=3, n_ao=10, n_grid1=400, n_grid2=1600, size_bh=9, seed=4)
+    Xo, Io = oracle.cutc_int(p)
+    errs = []
+    for S in (3, 4, 5):
+        X, I = cg.build_integrals(p, cg.SPLIT_BF16, n_slices=S)
+        errs.append(oracle.rel_err(I, Io)["norm"])
+    assert errs[0] > errs[1] > errs[2]
+    assert errs[2] < TOL_SPLIT
+
+
+def test_drop_in_env_selects_split(monkeypatch):
+    """CUTC_PRECISION=split switches the unmodified cutc_int entry point."""
+    p, ref = load_case("tiny_spd")
+    monkeypatch.setenv("CUTC_PRECISION", "split")
+    X = np.zeros((3, p.n_grid1, p.n_ao ** 2))
+    I = np.zeros((p.n_ao ** 2, p.n_ao ** 2))
+    s = cg.cutc_int(*[int(v) for v in ref["dims"]], p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc,
+                    p.size_bh, p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2,
+                    p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I)
+    assert s == 0, cg.last_error()
+    _check(X, I, ref["X"], ref["int2e"])

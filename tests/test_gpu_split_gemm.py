@@ -1,0 +1,89 @@
+"""The tcgen05 split-precision GEMM against an FP64 reference.
+
+Each operand row is cut into S signed 9-bit BF16 slices of its own scale
+(rounding error <= 2^-(9S) of the row maximum), so element (m, n) of the
+product is bounded by
+
+    |C - AB^T|_mn <= tol(S) * (max|A_m| |B_n|_1 + |A_m|_1 max|B_n|)
+
+with tol(S) = max(2^-(9S-3), 2^-44): the second value is the floor left by the
+FP32 running sum of the third slice diagonal, which is not accumulated exactly.
+"""
+import numpy as np
+import pytest
+
+import cutc_gb300 as cg
+
+pytestmark = pytest.mark.gpu
+
+
+def _ref(A, B):
+    return A @ B.T, np.abs(A) @ np.abs(B).T
+
+
+def _bound(A, B, S):
+    tol = max(2.0 ** -(9 * S - 3), 2.0 ** -44)
+    a_inf, b_inf = np.abs(A).max(axis=1), np.abs(B).max(axis=1)
+    a_1, b_1 = np.abs(A).sum(axis=1), np.abs(B).sum(axis=1)
+    return tol * (a_inf[:, None] * b_1[None, :] + a_1[:, None] * b_inf[None, :])
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (130, 70, 100), (300, 257, 1000),
+                                   (7, 5, 3), (1000, 200, 5000)])
+@pytest.mark.parametrize("S", [5])
+def test_split_gemm_random(M, N, K, S):
+    import torch
+    rng = np.random.default_rng(M * 7 + N * 3 + K)
+    A = rng.standard_normal((M, K)) * np.exp(rng.uniform(-5, 5, size=(M, 1)))
+    B = rng.standard_normal((N, K)) * np.exp(rng.uniform(-5, 5, size=(N, 1)))
+    C = cg.split_gemm_device(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda(), n_slices=S)
+    C = C.cpu().numpy()
+    R, Ab = _ref(A, B)
+    assert np.all(np.abs(C - R) <= _bound(A, B, S)), (np.abs(C - R) / _bound(A, B, S)).max()
+    # and in the usual dot-product scale
+    assert (np.abs(C - R) / Ab).max() < 2.0 ** -38
+
+
+@pytest.mark.parametrize("S", [3, 4, 6, 7])
+def test_split_gemm_slice_counts(S):
+    import torch
+    rng = np.random.default_rng(S)
+    M, N, K = 200, 100, 700
+    A = rng.standard_normal((M, K))
+    B = rng.standard_normal((N, K))
+    C = cg.split_gemm_device(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda(), n_slices=S)
+    R, Ab = _ref(A, B)
+    C = C.cpu().numpy()
+    assert np.all(np.abs(C - R) <= _bound(A, B, S)), (np.abs(C - R) / _bound(A, B, S)).max()
+
+
+def test_split_gemm_wide_dynamic_range_and_zeros():
+    """Rows spanning 2^-60..2^60, an all-zero row, exact zeros inside rows."""
+    import torch
+    rng = np.random.default_rng(3)
+    M, N, K = 150, 90, 2000
+    A = rng.standard_normal((M, K)) * np.exp2(rng.uniform(-60, 60, size=(M, K)))
+    B = rng.standard_normal((N, K))
+    A[5] = 0.0
+    B[:, ::7] = 0.0
+    C = cg.split_gemm_device(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda(), n_slices=5)
+    R, Ab = _ref(A, B)
+    C = C.cpu().numpy()
+    assert np.all(C[5] == 0.0)
+    # per element, against max|A_m| |B_n|_1 (tiny entries fall below the slices)
+    bound = np.abs(A).max(axis=1)[:, None] * np.abs(B).sum(axis=1)[None, :]
+    assert np.all(np.abs(C - R) <= 2.0 ** -40 * bound + 1e-300)
+
+
+def test_split_gemm_long_k_exact_accumulation():
+    """K = 2^17: exactness of the chunked accumulation keeps the error at the slice level."""
+    import torch
+    rng = np.random.default_rng(11)
+    M, N, K = 128, 64, 1 << 17
+    A = np.abs(rng.standard_normal((M, K)))  # same signs: worst case for accumulation
+    B = np.abs(rng.standard_normal((N, K)))
+    C = cg.split_gemm_device(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda(), n_slices=5)
+    R, Ab = _ref(A, B)
+    C = C.cpu().numpy()
+    assert np.all(np.abs(C - R) <= _bound(A, B, 5))
+    assert (np.abs(C - R) / Ab).max() < 2.0 ** -40
