@@ -234,6 +234,7 @@ static int validate(const Request &R)
 enum Slot {
     S_R1, S_WR1, S_R2, S_WR2, S_RN, S_AOS1, S_AOS2, S_COEF, S_EXPS, S_OFF,
     S_T1, S_F2, S_P, S_G, S_XP, S_S0, S_SL, S_H, S_N, S_XOUT, S_IOUT,
+    S_R2D, S_F2D, S_POLY,
     S_SPLIT0  // split-form slots follow
 };
 
@@ -342,6 +343,19 @@ int run_build(Engine *E, const Request &R, cutc_stats *stats)
     note_launches(1);
 
     SplitPlan sp;
+    float2 *d_r2d = nullptr, *d_f2d = nullptr, *d_poly = nullptr;
+    int pexp = 4;
+    if (R.precision == CUTC_SPLIT_BF16) {
+        pexp = pair_df_max_exp(exps.data(), nt);
+        CUTC_TRY(W.get(S_R2D, 3 * (size_t)n2 * sizeof(float2), &p));
+        d_r2d = (float2 *)p;
+        CUTC_TRY(W.get(S_F2D, (size_t)nN * n2 * sizeof(float2), &p));
+        d_f2d = (float2 *)p;
+        CUTC_TRY(W.get(S_POLY, pair_df_poly_bytes(pexp, (int)n1t, nN), &p));
+        d_poly = (float2 *)p;
+        CUTC_TRY(launch_r2_df(st, n2, nN, d_r2, d_f2, d_r2d, d_f2d));
+        note_launches(1);
+    }
     if (R.precision == CUTC_PLAIN_FP64) {
         CUTC_TRY(W.get(S_P, (size_t)np * n2 * 8, &p));
         d_P = (double *)p;
@@ -359,16 +373,30 @@ int run_build(Engine *E, const Request &R, cutc_stats *stats)
         const int i0 = (int)(tile * n1t);
         const int nb = (int)std::min<int64_t>(n1t, n1 - i0);
         CUTC_TRY(launch_r1_terms(st, i0, nb, nN, d_r1, d_rn, R.a_en, d_t1));
-        PairArgs P;
-        P.i0 = i0; P.n1b = nb; P.n2 = n2; P.nN = nN; P.n_terms = nt;
-        P.r1 = d_r1; P.r2 = d_r2; P.t1 = d_t1; P.f2 = d_f2;
-        P.coef = d_coef; P.exps = d_exps; P.term_off = d_off;
-        P.a_ee = R.a_ee;
-        P.G = d_G; P.ldg = n2; P.plane = (int64_t)nb * n2;
         CUTC_CUDA_TRY(cudaEventRecord(E->ev[3], st));
-        CUTC_TRY(launch_pair_f64(st, P));
+        if (R.precision == CUTC_PLAIN_FP64) {
+            PairArgs P;
+            P.i0 = i0; P.n1b = nb; P.n2 = n2; P.nN = nN; P.n_terms = nt;
+            P.r1 = d_r1; P.r2 = d_r2; P.t1 = d_t1; P.f2 = d_f2;
+            P.coef = d_coef; P.exps = d_exps; P.term_off = d_off;
+            P.a_ee = R.a_ee;
+            P.G = d_G; P.ldg = n2; P.plane = (int64_t)nb * n2;
+            CUTC_TRY(launch_pair_f64(st, P));
+            note_launches(2);
+        } else {
+            PairDfArgs P;
+            P.i0 = i0; P.n1b = nb; P.n2 = n2; P.nN = nN; P.rows_per_cta = 0;
+            P.r1 = d_r1; P.r2 = d_r2; P.r2d = d_r2d; P.f2 = d_f2; P.f2d = d_f2d; P.t1 = d_t1;
+            P.poly = d_poly; P.poly_w = d_poly;
+            P.coef = d_coef; P.exps = d_exps; P.term_off = d_off;
+            P.a_ee = R.a_ee;
+            P.a_ee_hi = (float)R.a_ee;
+            P.a_ee_lo = (float)(R.a_ee - (double)P.a_ee_hi);
+            P.G = reinterpret_cast<float2 *>(d_G); P.ldg = n2; P.plane = (int64_t)nb * n2;
+            CUTC_TRY(launch_pair_df(st, P, pexp, d_rn, R.a_en));
+            note_launches(3);
+        }
         CUTC_CUDA_TRY(cudaEventRecord(E->ev[4], st));
-        note_launches(2);
         if (R.precision == CUTC_PLAIN_FP64) {
             // Xp[(m n1 + i0 + i) np + p] = sum_g P[p n2 + g] G[m plane + i n2 + g]
             const double one = 1.0, zero = 0.0;
@@ -377,7 +405,7 @@ int run_build(Engine *E, const Request &R, cutc_stats *stats)
                 (long long)nb * n2, &zero, d_Xp + (int64_t)i0 * np, (int)np,
                 (long long)n1 * np, 4));
         } else {
-            CUTC_TRY(split_x_tile(E, R, st, sp, d_G, i0, nb, d_Xp));
+            CUTC_TRY(split_x_tile(E, R, st, sp, reinterpret_cast<const float2 *>(d_G), i0, nb, d_Xp));
         }
         if (stats) {
             CUTC_CUDA_TRY(cudaEventSynchronize(E->ev[4]));

@@ -30,6 +30,34 @@ struct PairArgs {
     int64_t plane;
 };
 
+// Arguments of the double-float pair kernel (split form).
+struct PairDfArgs {
+    int i0, n1b, n2, nN;
+    int rows_per_cta;       // set by the launcher
+    const double *r1;       // (3, n_grid1) AoS, FP64
+    const double *r2;       // (3, n2) AoS, FP64 (near-coalescence path)
+    const float2 *r2d;      // [3][n2] df coordinates
+    const double *f2;       // [nN][n2] FP64 (near-coalescence path)
+    const float2 *f2d;      // [nN][n2] df
+    const NucTerm *t1;      // [n1b][nN] FP64 per-point terms (near-coalescence path)
+    const float2 *poly;     // [n1b][nN][kN] df polynomial coefficients (written by the launcher)
+    float2 *poly_w;
+    const double *coef;     // term table, as PairArgs
+    const int *exps;
+    const int *term_off;
+    double a_ee;            // FP64 (near path)
+    float a_ee_hi, a_ee_lo; // df
+    float2 *G;              // G[c * plane + i * ldg + j] as (hi, lo)
+    int64_t ldg;
+    int64_t plane;
+};
+
+int pair_df_max_exp(const int *exps, int n_terms);
+size_t pair_df_poly_bytes(int E, int n1b, int nN);
+int launch_r2_df(cudaStream_t st, int n2, int nN, const double *r2, const double *f2, float2 *r2d,
+                 float2 *f2d);
+int launch_pair_df(cudaStream_t st, const PairDfArgs &P, int E, const double *rn, double a_en);
+
 int launch_r1_terms(cudaStream_t st, int i0, int n, int nN, const double *r1, const double *rn,
                     double a, NucTerm *t1);
 int launch_r2_terms(cudaStream_t st, int n2, int nN, const double *r2, const double *rn,

@@ -1,0 +1,328 @@
+// Pair terms grad1 u(r1, r2) in double-float arithmetic (split form, sm_103a).
+//
+// Same quantity as pair.cu (the reference's cutc_int_bh_kernel,
+// src/jast_bh.cu:31-264), reorganised so that the O(n1 n2) part runs on the
+// FP32 pipes, which issue 64x faster than FP64 on GB300:
+//
+//   For nucleus A the Jastrow terms give two polynomials in (f2A, g12),
+//     du/df1A = sum_{b,o} U_A[b][o](r1) f2A^b g^o
+//     du/dg   = sum_A sum_{b,o'} W_A[b][o'](r1) f2A^b g^o'
+//   with the r1-dependent coefficients
+//     U[n][o] += c m f1^{m-1},  U[m][o] += c n f1^{n-1}
+//     W[n][o-1] += c o f1^m,    W[m][o-1] += c o f1^n       (term (c, m, n, o))
+//   computed once per (r1, nucleus) in FP64 by r1_poly_kernel.  Per pair the
+//   kernel evaluates both polynomials by Horner's rule in df arithmetic
+//   (~43 df multiply-adds per nucleus for exponents <= 4), then
+//     grad1 u = sum_A du/df1A grad f1A + du/dg grad g12.
+//   * Pairs closer than 0.01 bohr (e-e coalescence) are evaluated entirely in
+//     FP64 with the reference's own term-by-term formula and its r^2 > 1e-15
+//     guard; e-n coalescence is handled by the FP64 per-point terms.
+//   * Output is G[c][i][j] as (hi, lo) float pairs; hi + lo is exact in FP64.
+#include <algorithm>
+
+#include "common.cuh"
+#include "dfloat.cuh"
+#include "pair.cuh"
+
+namespace cutc {
+
+constexpr int kDfThreads = 128;
+constexpr float kNearR2 = 1.0e-4f;  // r12^2 below which a pair is done in FP64
+
+template <int E>
+struct PolyLayout {
+    static constexpr int kU = (E + 1) * (E + 1);  // U[b][o]
+    static constexpr int kW = (E + 1) * E;        // W[b][o'], o' = o - 1
+    static constexpr int kN = kU + kW + 3;        // + grad f1 (x, y, z)
+};
+
+// coef[(i * nN + A) * kN + ...] for rows i of the tile, in df
+template <int E>
+__global__ void r1_poly_kernel(int i0, int n, int nN, const double *__restrict__ r1,
+                               const double *__restrict__ rn, double a_en,
+                               const double *__restrict__ tcoef, const int *__restrict__ texps,
+                               const int *__restrict__ toff, float2 *__restrict__ out)
+{
+    using L = PolyLayout<E>;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * nN)
+        return;
+    const int i = (int)(idx / nN), A = (int)(idx % nN);
+    const double *p = r1 + 3 * (int64_t)(i0 + i);
+    const double dx = p[0] - rn[3 * A], dy = p[1] - rn[3 * A + 1], dz = p[2] - rn[3 * A + 2];
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    double f = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+    if (d2 > 1e-15) {
+        const double d = sqrt(d2);
+        const double t = 1.0 / (1.0 + a_en * d);
+        f = a_en * d * t;
+        const double s = a_en * t * t / d;
+        gx = s * dx;
+        gy = s * dy;
+        gz = s * dz;
+    }
+    double F[kMaxExp + 1];
+    F[0] = 1.0;
+    for (int k = 1; k <= kMaxExp; k++)
+        F[k] = F[k - 1] * f;
+    double U[L::kU], W[L::kW];
+    for (int k = 0; k < L::kU; k++)
+        U[k] = 0.0;
+    for (int k = 0; k < L::kW; k++)
+        W[k] = 0.0;
+    for (int k = toff[A]; k < toff[A + 1]; k++) {
+        const int e = texps[k];
+        const int m = e & 7, nn = (e >> 3) & 7, o = (e >> 6) & 7;
+        const double cm = tcoef[3 * k], cn = tcoef[3 * k + 1], co = tcoef[3 * k + 2];
+        if (m > 0)
+            U[nn * (E + 1) + o] += cm * F[m - 1];
+        if (nn > 0)
+            U[m * (E + 1) + o] += cn * F[nn - 1];
+        if (o > 0) {
+            W[nn * E + o - 1] += co * F[m];
+            W[m * E + o - 1] += co * F[nn];
+        }
+    }
+    float2 *dst = out + idx * L::kN;
+    for (int k = 0; k < L::kU; k++) {
+        const df::D v = df::from_double(U[k]);
+        dst[k] = make_float2(v.hi, v.lo);
+    }
+    for (int k = 0; k < L::kW; k++) {
+        const df::D v = df::from_double(W[k]);
+        dst[L::kU + k] = make_float2(v.hi, v.lo);
+    }
+    const double gg[3] = {gx, gy, gz};
+    for (int c = 0; c < 3; c++) {
+        const df::D v = df::from_double(gg[c]);
+        dst[L::kU + L::kW + c] = make_float2(v.hi, v.lo);
+    }
+}
+
+// r2 coordinates and f2A in df: r2d[c * n2 + j], f2d[A * n2 + j]
+__global__ void r2_df_kernel(int n2, int nN, const double *__restrict__ r2,
+                             const double *__restrict__ f2, float2 *__restrict__ r2d,
+                             float2 *__restrict__ f2d)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n2)
+        return;
+    for (int c = 0; c < 3; c++) {
+        const df::D v = df::from_double(r2[3 * (int64_t)j + c]);
+        r2d[(int64_t)c * n2 + j] = make_float2(v.hi, v.lo);
+    }
+    for (int A = 0; A < nN; A++) {
+        const df::D v = df::from_double(f2[(int64_t)A * n2 + j]);
+        f2d[(int64_t)A * n2 + j] = make_float2(v.hi, v.lo);
+    }
+}
+
+// One pair in FP64, term by term as the reference kernel does it
+// (src/jast_bh.cu:138-254), for pairs near e-e coalescence.
+__device__ __noinline__ void pair_fp64_single(const PairDfArgs &P, int i, int j, double out[4])
+{
+    const int64_t gi = P.i0 + i;
+    const double dx = P.r1[3 * gi] - P.r2[3 * (int64_t)j];
+    const double dy = P.r1[3 * gi + 1] - P.r2[3 * (int64_t)j + 1];
+    const double dz = P.r1[3 * gi + 2] - P.r2[3 * (int64_t)j + 2];
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    const double a = P.a_ee;
+    double g = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+    if (d2 > 1e-15) {
+        const double d = sqrt(d2);
+        const double t = 1.0 / (1.0 + a * d);
+        g = a * d * t;
+        const double s = a * t * t / d;
+        gx = s * dx;
+        gy = s * dy;
+        gz = s * dz;
+    }
+    double ux = 0.0, uy = 0.0, uz = 0.0;
+    for (int A = 0; A < P.nN; A++) {
+        const NucTerm t1 = P.t1[(int64_t)i * P.nN + A];
+        const double f1 = t1.f, f2 = P.f2[(int64_t)A * P.n2 + j];
+        for (int k = P.term_off[A]; k < P.term_off[A + 1]; k++) {
+            const int e = P.exps[k];
+            const int m = e & 7, n = (e >> 3) & 7, o = (e >> 6) & 7;
+            double F1[kMaxExp + 1], F2[kMaxExp + 1], Gp[kMaxExp + 1];
+            F1[0] = F2[0] = Gp[0] = 1.0;
+            for (int q = 1; q <= kMaxExp; q++) {
+                F1[q] = F1[q - 1] * f1;
+                F2[q] = F2[q - 1] * f2;
+                Gp[q] = Gp[q - 1] * g;
+            }
+            double t1v = 0.0, t2v = 0.0;
+            if (m > 0)
+                t1v += P.coef[3 * k] * F1[m - 1] * F2[n];
+            if (n > 0)
+                t1v += P.coef[3 * k + 1] * F1[n - 1] * F2[m];
+            t1v *= Gp[o];
+            if (o > 0)
+                t2v = P.coef[3 * k + 2] * Gp[o - 1] * (F1[m] * F2[n] + F1[n] * F2[m]);
+            ux += t1v * t1.gx + t2v * gx;
+            uy += t1v * t1.gy + t2v * gy;
+            uz += t1v * t1.gz + t2v * gz;
+        }
+    }
+    out[0] = ux;
+    out[1] = uy;
+    out[2] = uz;
+    out[3] = -0.5 * (ux * ux + uy * uy + uz * uz);
+}
+
+template <int E>
+__global__ void __launch_bounds__(kDfThreads)
+pair_df_kernel(PairDfArgs P)
+{
+    using L = PolyLayout<E>;
+    extern __shared__ __align__(16) float2 s_coef[];  // [row][A][kN], then r1 df [row][3]
+    const int rows = P.rows_per_cta;
+    const int row0 = blockIdx.y * rows;
+    const int nrows = min(rows, P.n1b - row0);
+    const int per_row = P.nN * L::kN;
+    float2 *s_r1 = s_coef + rows * per_row;
+    for (int k = threadIdx.x; k < nrows * per_row; k += kDfThreads)
+        s_coef[k] = P.poly[(int64_t)row0 * per_row + k];
+    for (int k = threadIdx.x; k < nrows * 3; k += kDfThreads) {
+        const int r = k / 3, c = k % 3;
+        const df::D v = df::from_double(P.r1[3 * (int64_t)(P.i0 + row0 + r) + c]);
+        s_r1[k] = make_float2(v.hi, v.lo);
+    }
+    __syncthreads();
+
+    const int j = blockIdx.x * kDfThreads + threadIdx.x;
+    if (j >= P.n2)
+        return;
+    const float2 x2 = P.r2d[j], y2 = P.r2d[P.n2 + j], z2 = P.r2d[2 * (int64_t)P.n2 + j];
+    const df::D a = df::make(P.a_ee_hi, P.a_ee_lo);
+
+    for (int r = 0; r < nrows; r++) {
+        const float2 *rr = s_r1 + 3 * r;
+        const df::D dx = df::sub(df::make(rr[0].x, rr[0].y), df::make(x2.x, x2.y));
+        const df::D dy = df::sub(df::make(rr[1].x, rr[1].y), df::make(y2.x, y2.y));
+        const df::D dz = df::sub(df::make(rr[2].x, rr[2].y), df::make(z2.x, z2.y));
+        const df::D d2 = df::add(df::add(df::sqr(dx), df::sqr(dy)), df::sqr(dz));
+        const int64_t o = (int64_t)(row0 + r) * P.ldg + j;
+        if (d2.hi < kNearR2) {
+            double v[4];
+            pair_fp64_single(P, row0 + r, j, v);
+            for (int c = 0; c < 4; c++) {
+                const df::D w = df::from_double(v[c]);
+                P.G[o + c * P.plane] = make_float2(w.hi, w.lo);
+            }
+            continue;
+        }
+        // g = a r / (1 + a r), grad g = a / (r (1 + a r)^2) (r1 - r2)
+        const df::D rd = df::sqrt(d2);
+        const df::D ar = df::mul(rd, a);
+        const df::D t = df::recip(df::add_f(ar, 1.0f));
+        const df::D g = df::mul(ar, t);
+        const df::D s = df::mul(df::mul(df::sqr(t), a), df::recip(rd));
+        const df::D gx = df::mul(s, dx), gy = df::mul(s, dy), gz = df::mul(s, dz);
+
+        df::D ux = {0.f, 0.f}, uy = {0.f, 0.f}, uz = {0.f, 0.f}, dudg = {0.f, 0.f};
+        const float2 *cr = s_coef + r * per_row;
+        for (int A = 0; A < P.nN; A++) {
+            const float2 f2v = P.f2d[(int64_t)A * P.n2 + j];
+            const df::D f2 = df::make(f2v.x, f2v.y);
+            const float2 *U = cr + A * L::kN;
+            const float2 *W = U + L::kU;
+            // du/df1A = sum_b f2^b (sum_o U[b][o] g^o)
+            df::D acc = {0.f, 0.f};
+#pragma unroll
+            for (int b = E; b >= 0; b--) {
+                df::D in = df::make(U[b * (E + 1) + E].x, U[b * (E + 1) + E].y);
+#pragma unroll
+                for (int q = E - 1; q >= 0; q--)
+                    in = df::fma(in, g, df::make(U[b * (E + 1) + q].x, U[b * (E + 1) + q].y));
+                acc = (b == E) ? in : df::fma(acc, f2, in);
+            }
+            // du/dg contribution = sum_b f2^b (sum_o' W[b][o'] g^o')
+            df::D acw = {0.f, 0.f};
+#pragma unroll
+            for (int b = E; b >= 0; b--) {
+                df::D in = df::make(W[b * E + E - 1].x, W[b * E + E - 1].y);
+#pragma unroll
+                for (int q = E - 2; q >= 0; q--)
+                    in = df::fma(in, g, df::make(W[b * E + q].x, W[b * E + q].y));
+                acw = (b == E) ? in : df::fma(acw, f2, in);
+            }
+            const float2 *gf = W + L::kW;
+            ux = df::fma(acc, df::make(gf[0].x, gf[0].y), ux);
+            uy = df::fma(acc, df::make(gf[1].x, gf[1].y), uy);
+            uz = df::fma(acc, df::make(gf[2].x, gf[2].y), uz);
+            dudg = df::add(dudg, acw);
+        }
+        ux = df::fma(dudg, gx, ux);
+        uy = df::fma(dudg, gy, uy);
+        uz = df::fma(dudg, gz, uz);
+        const df::D n2v = df::add(df::add(df::sqr(ux), df::sqr(uy)), df::sqr(uz));
+        const df::D l = df::mul_f(n2v, -0.5f);
+        P.G[o] = make_float2(ux.hi, ux.lo);
+        P.G[o + P.plane] = make_float2(uy.hi, uy.lo);
+        P.G[o + 2 * P.plane] = make_float2(uz.hi, uz.lo);
+        P.G[o + 3 * P.plane] = make_float2(l.hi, l.lo);
+    }
+}
+
+int pair_df_max_exp(const int *exps, int n_terms)
+{
+    int E = 0;
+    for (int k = 0; k < n_terms; k++) {
+        const int e = exps[k];
+        E = max(E, max(e & 7, max((e >> 3) & 7, (e >> 6) & 7)));
+    }
+    return E <= 4 ? 4 : 6;
+}
+
+size_t pair_df_poly_bytes(int E, int n1b, int nN)
+{
+    const int kN = E == 4 ? PolyLayout<4>::kN : PolyLayout<6>::kN;
+    return (size_t)n1b * nN * kN * sizeof(float2);
+}
+
+int launch_r2_df(cudaStream_t st, int n2, int nN, const double *r2, const double *f2, float2 *r2d,
+                 float2 *f2d)
+{
+    r2_df_kernel<<<ceil_div(n2, 256), 256, 0, st>>>(n2, nN, r2, f2, r2d, f2d);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    return CUTC_OK;
+}
+
+template <int E>
+static int launch_df_impl(cudaStream_t st, PairDfArgs P, const double *rn, double a_en)
+{
+    using L = PolyLayout<E>;
+    const int64_t total = (int64_t)P.n1b * P.nN;
+    r1_poly_kernel<E><<<ceil_div(total, 128), 128, 0, st>>>(P.i0, P.n1b, P.nN, P.r1, rn, a_en,
+                                                            P.coef, P.exps, P.term_off, P.poly_w);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    const size_t per_row = (size_t)P.nN * L::kN * sizeof(float2) + 3 * sizeof(float2);
+    const size_t budget = 160 * 1024;
+    int rows = (int)std::min<size_t>(8, budget / per_row);
+    if (rows < 1) {
+        cutc_set_error(CUTC_ERR_INVALID, "too many nuclei for the df pair kernel");
+        return CUTC_ERR_INVALID;
+    }
+    P.rows_per_cta = rows;
+    const size_t smem = rows * per_row;
+    static bool attr = false;
+    if (!attr) {
+        CUTC_CUDA_TRY(cudaFuncSetAttribute(pair_df_kernel<E>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        attr = true;
+    }
+    dim3 grid(ceil_div(P.n2, kDfThreads), ceil_div(P.n1b, rows));
+    pair_df_kernel<E><<<grid, kDfThreads, smem, st>>>(P);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    return CUTC_OK;
+}
+
+int launch_pair_df(cudaStream_t st, const PairDfArgs &P, int E, const double *rn, double a_en)
+{
+    if (P.n1b <= 0 || P.n2 <= 0)
+        return CUTC_OK;
+    return E == 4 ? launch_df_impl<4>(st, P, rn, a_en) : launch_df_impl<6>(st, P, rn, a_en);
+}
+
+}  // namespace cutc

@@ -341,6 +341,16 @@ struct SrcDense {  // X[r * ld + k]
     __device__ double operator()(int64_t r, int64_t k) const { return X[r * ld + k]; }
 };
 
+struct SrcDenseDF {  // hi + lo of X[r * ld + k] (exact in FP64)
+    const float2 *X;
+    int64_t ld;
+    __device__ double operator()(int64_t r, int64_t k) const
+    {
+        const float2 v = X[r * ld + k];
+        return (double)v.x + (double)v.y;
+    }
+};
+
 struct SrcSym {  // w[k] chi_a(k) chi_b(k), (a, b) = pairs[r]
     const double *w, *chi;
     int64_t ldchi;
@@ -734,7 +744,7 @@ int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *
     return CUTC_OK;
 }
 
-int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const double *G,
+int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const float2 *G,
                  int i0, int nb, double *Xp)
 {
     (void)E;
@@ -743,9 +753,9 @@ int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, co
     B.M = 4 * nb;  // rows (c, i) of this tile; Mpad keeps the allocated padding
     B.Mpad = (int)round_up(B.M, kBN);
     const int64_t np = n_pairs(R.nA);
-    SrcDense src{G, (int64_t)R.n2};
+    SrcDenseDF src{G, (int64_t)R.n2};
     CUTC_SLICES_DISPATCH(sp.n_slices, {
-        CUTC_TRY((slice_rows<S, SrcDense>(st, src, B)));
+        CUTC_TRY((slice_rows<S, SrcDenseDF>(st, src, B)));
         CUTC_TRY((gemm<S>(st, S_.AX, B, 1.0, Xp, np, nb, R.n1, i0, 0, S_.err)));
     });
     return CUTC_OK;

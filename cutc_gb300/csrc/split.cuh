@@ -34,7 +34,8 @@ struct SplitPlan {
 size_t split_r1_row_bytes(const Request &R);
 int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *wr2,
                     const double *aos2v, int64_t n1t, int slot0, SplitPlan &sp);
-int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const double *G,
+// G is the df tile G[c][i][j] as (hi, lo) float pairs
+int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const float2 *G,
                  int i0, int nb, double *Xp);
 int split_int2e(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const double *wr1,
                 const double *aos1, const double *Xp, double *I);
