@@ -1,0 +1,417 @@
+"""Throughput of the cutc_int hot path on GB300: TC-integral builds per second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config medium] [--precision split|plain]
+
+One step is one full integral build (pair terms, X, int_2e) of the named
+workload.  ``value`` is builds/s with inputs and outputs resident in HBM
+(device pointers through cutc_int_ex); ``e2e`` is the same metric through the
+C-ABI with host buffers, host<->device copies inside the timed region.
+``--impl reference`` times the CPU restatement of the reference's formulas
+(oracle/, OpenMP C + numpy/OpenBLAS DGEMM) on the host cores: the reference
+ships no CPU path, so its arithmetic is transcribed and timed on a bounded
+sample of r1 rows, scaled to a full build.
+
+Under torchrun (N > 1) every rank runs an independent replica of the workload
+(the path is single-GPU; there is no collective on the data path) and the
+reported value is the sum over ranks: weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from cutc_gb300 import synth  # noqa: E402
+
+METRIC = "TC integral builds/s (split-precision vs FP64 at 1e-10 rel err)"
+UNIT = "builds/s"
+CPU_SAMPLE_ROWS = 48
+
+
+def log(msg):
+    print("[bench %.1fs] %s" % (time.perf_counter() - _T0, msg), file=sys.stderr, flush=True)
+
+
+_T0 = time.perf_counter()
+
+
+def workload_desc(name, p):
+    return ("%s: %d nuclei, n_ao=%d, n_grid1=%d, n_grid2=%d, %d Jastrow terms/atom"
+            % (name, p.n_nuc, p.n_ao, p.n_grid1, p.n_grid2, p.size_bh))
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def sub_problem(p, i0, n):
+    """The same molecule with r1 restricted to rows [i0, i0+n)."""
+    import dataclasses
+    return dataclasses.replace(
+        p, r1=np.ascontiguousarray(p.r1[i0:i0 + n]), wr1=np.ascontiguousarray(p.wr1[i0:i0 + n]),
+        aos1=np.ascontiguousarray(p.aos1[:, :, i0:i0 + n]))
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id=None):
+        self.lines = []
+        self.proc = None
+        self.gpu_id = gpu_id
+
+    def start(self):
+        cmd = ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+               "-lms", "200"]
+        if self.gpu_id:
+            cmd += ["-i", self.gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle leg (bounded sample)
+# ---------------------------------------------------------------------------
+def cpu_sample(p, rows=CPU_SAMPLE_ROWS, reps=1, offsets=(0,)):
+    """Time the oracle on `rows` r1 rows (pair terms, X, their int_2e share)
+    plus the r2-side products once; scale to the full build."""
+    from oracle import oracle
+    t0 = time.perf_counter()
+    P = oracle.long_range(p)
+    t_p = time.perf_counter() - t0
+    times = []
+    for rep in range(reps):
+        i0 = offsets[rep % len(offsets)]
+        sub = sub_problem(p, i0, rows)
+        t0 = time.perf_counter()
+        X = oracle.x_block(sub, P, 0, rows)
+        oracle.int2e_from_x(sub, X)
+        times.append(time.perf_counter() - t0)
+    t_rows = float(np.mean(times))
+    t_build = t_p + t_rows * p.n_grid1 / rows
+    return {
+        "value": 1.0 / t_build,
+        "unit": UNIT,
+        "cores": os.cpu_count(),
+        "kind": "port",
+        "sample": ("%d of %d r1 rows (pair terms, X rows and their int_2e share, "
+                   "%d rep(s)) + the r2 pair products once; scaled by n_grid1/%d"
+                   % (rows, p.n_grid1, reps, rows)),
+        "seconds_timed": t_p + sum(times),
+    }, t_rows, t_p
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference path, rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    p = synth.make_config(args.config)
+    from oracle import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    P = oracle.long_range(p)
+    t_p = time.perf_counter() - t0
+    rows = CPU_SAMPLE_ROWS
+    step_times = []
+    for step in range(args.warmup + args.steps):
+        i0 = (step * 997 * rows) % max(1, p.n_grid1 - rows)
+        sub = sub_problem(p, i0, rows)
+        t0 = time.perf_counter()
+        X = oracle.x_block(sub, P, 0, rows)
+        oracle.int2e_from_x(sub, X)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            step_times.append(dt)
+    t_rows = float(np.mean(step_times))
+    t_build = t_p + t_rows * p.n_grid1 / rows
+    value = 1.0 / t_build
+    cb = {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+          "sample": ("each step: %d of %d r1 rows (pair terms, X rows, their int_2e share); "
+                     "r2 pair products timed once; scaled by n_grid1/%d"
+                     % (rows, p.n_grid1, rows))}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_build * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_desc(args.config, p), "precision": "fp64 (CPU)"},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import cutc_gb300 as cg
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
+    p = synth.make_config(args.config)
+
+    # ---- device-resident arrays ------------------------------------------------
+    def d(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    dr = {k: d(v) for k, v in p.arrays().items()}
+    nA2 = p.n_ao ** 2
+    Xd = torch.empty((3, p.n_grid1, nA2), dtype=torch.float64, device=dev)
+    Id = torch.empty((nA2, nA2), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    opt = cg.options(prec, args.slices, p.a_en, p.a_ee, 3, True, 0, stream.cuda_stream)
+
+    def build_device(stats=None):
+        s = cg.cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                           dr["r1"], dr["wr1"], dr["r2"], dr["wr2"], dr["rn"], dr["aos1"], dr["aos2"],
+                           dr["c_bh"], dr["m_bh"], dr["n_bh"], dr["o_bh"], Xd, Id, stats)
+        if s != cg.CUTC_OK:
+            raise cg.CutcError(s, cg.last_error())
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    log("inputs on device; warm-up")
+    for _ in range(args.warmup):
+        build_device()
+    log("timed region")
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        uuid = None
+    sampler = ClockSampler(uuid)
+    sampler.start()
+    time.sleep(0.5)
+    barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    gemm_ms, gemm_launches, launches, pair_ms = 0.0, 0, 0, 0.0
+    for _ in range(args.steps):
+        st = cg.Stats()
+        build_device(st)
+        gemm_ms += st.ms_x_gemm
+        gemm_launches += st.n_x_gemm
+        launches += st.gpu_launches
+        pair_ms += st.ms_pair
+    ev1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    t = torch.tensor([elapsed_ms], dtype=torch.float64, device=dev)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    elapsed_ms = float(t.item())
+    ms_per_step = elapsed_ms / args.steps
+    value = world * args.steps / (elapsed_ms / 1e3)
+
+    # ---- end to end through the C-ABI with host buffers -------------------------
+    def pinned(a):
+        t_ = torch.empty(a.shape, dtype=torch.from_numpy(np.empty(0, a.dtype)).dtype, pin_memory=True)
+        t_.numpy()[...] = a
+        return t_.numpy()
+
+    log("device-resident: %.3f builds/s; end-to-end leg" % value)
+    hp = {k: pinned(v) for k, v in p.arrays().items()}
+    Xh = torch.empty((3, p.n_grid1, nA2), dtype=torch.float64, pin_memory=True).numpy()
+    Ih = torch.empty((nA2, nA2), dtype=torch.float64, pin_memory=True).numpy()
+    opt_h = cg.options(prec, args.slices, p.a_en, p.a_ee, 3, False, 0, stream.cuda_stream)
+
+    def build_host():
+        s = cg.cutc_int_ex(opt_h, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                           hp["r1"], hp["wr1"], hp["r2"], hp["wr2"], hp["rn"], hp["aos1"], hp["aos2"],
+                           hp["c_bh"], hp["m_bh"], hp["n_bh"], hp["o_bh"], Xh, Ih, None)
+        if s != cg.CUTC_OK:
+            raise cg.CutcError(s, cg.last_error())
+
+    build_host()
+    barrier()
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        build_host()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if dist is not None:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world * e2e_steps / float(te.item())
+    h2d = (p.r1.nbytes + p.wr1.nbytes + p.r2.nbytes + p.wr2.nbytes + p.rn.nbytes + p.aos1.nbytes
+           + p.aos2.nbytes // 4 + p.c_bh.nbytes + 3 * p.m_bh.nbytes)
+    d2h = Xh.nbytes + Ih.nbytes
+
+    out = None
+    if rank == 0:
+        peaks, peak_kind = measured_peaks()
+        alg_flops_x = 8.0 * nA2 * p.n_grid1 * p.n_grid2  # per build, dense formula
+        per_launch_flops = alg_flops_x * args.steps / max(1, gemm_launches)
+        per_launch_ms = gemm_ms / max(1, gemm_launches)
+        achieved = per_launch_flops / (per_launch_ms * 1e-3) / 1e12
+        peak = float(peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops")))
+        S = args.slices
+        n_products = S * (S + 1) // 2 if prec == cg.SPLIT_BF16 else 0
+        packed = p.n_ao * (p.n_ao + 1) / 2.0 / nA2
+        executed = achieved * packed * n_products if n_products else None
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak, "traffic": traffic_per_launch(args, p, gemm_launches),
+                    "kernel": "split_gemm_kernel (X build, one launch per r1 tile)",
+                    "peak_source": "bf16_tflops_sustained of %s" % peak_kind,
+                    "alg_flops_per_launch": per_launch_flops, "ms_per_launch": per_launch_ms,
+                    "executed_bf16_tflops": executed,
+                    "executed_frac": (executed / peak) if executed else None,
+                    "note": ("achieved counts the dense FP64 formula 8 nA^2 n1 n2; the kernel "
+                             "executes %d BF16 slice products on the packed (a>=b) AO pairs"
+                             % n_products)}
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
+               "config": {"workload": workload_desc(args.config, p),
+                          "precision": args.precision, "n_slices": S if prec else None,
+                          "l2": "inputs larger than L2: per-build working set of tens of GB",
+                          "parallelism": "replicas" if world > 1 else "1 GPU"},
+               "gpu_launches": launches,
+               "clocks": clocks,
+               "roofline": roofline,
+               "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                       "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+                       "buffers": "pinned host memory through cutc_int_ex"},
+               "phases_ms_per_step": {"pair": pair_ms / args.steps,
+                                      "x_gemm": gemm_ms / args.steps}}
+    # ---- accuracy and the plain FP64 rate on an r1 sample --------------------------
+    log("e2e: %.3f builds/s" % e2e_value)
+    if rank == 0 and not args.skip_accuracy:
+        log("accuracy / plain sample")
+        rows = 256
+        sub = sub_problem(p, (p.n_grid1 // 2) // 64 * 64, rows)
+        Xs, Is = cg.build_integrals(sub, cg.SPLIT_BF16, n_slices=args.slices)
+        cg.build_integrals(sub, cg.PLAIN_FP64)
+        t0 = time.perf_counter()
+        Xp, Ip = cg.build_integrals(sub, cg.PLAIN_FP64)
+        t_plain = time.perf_counter() - t0
+        from oracle.oracle import rel_err
+        out["accuracy"] = {"X_vs_fp64": rel_err(Xs, Xp), "int2e_vs_fp64": rel_err(Is, Ip),
+                           "sample": "%d of %d r1 rows of the workload; split (%d slices) vs "
+                                     "the plain FP64 form (itself 1e-12 from the oracle)"
+                                     % (rows, p.n_grid1, args.slices)}
+        out["plain_fp64"] = {"value_est": 1.0 / (t_plain * p.n_grid1 / rows), "unit": UNIT,
+                             "basis": "plain FP64 form on %d r1 rows (host buffers), scaled by "
+                                      "n_grid1/%d" % (rows, rows)}
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        log("cpu baseline sample")
+        cb, _, _ = cpu_sample(p)
+        out["cpu_baseline"] = cb
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def traffic_per_launch(args, p, launches):
+    """DRAM bytes per X-contraction launch from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "split_gemm_traffic.json")
+    if not os.path.exists(path):
+        return None
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        # bytes per (M x N x K) unit measured on the captured launch, scaled to this launch
+        per_unit = float(d["dram_bytes_per_mnk"])
+        np_ = p.n_ao * (p.n_ao + 1) // 2
+        n_per_launch = 4.0 * p.n_grid1 / max(1, launches / max(1, args.steps))
+        return per_unit * np_ * n_per_launch * p.n_grid2
+    except Exception:
+        return None
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="medium", choices=sorted(synth.CONFIGS))
+    ap.add_argument("--precision", choices=["split", "plain"], default="split")
+    ap.add_argument("--slices", type=int, default=5)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-accuracy", action="store_true")
+    args = ap.parse_args(argv)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

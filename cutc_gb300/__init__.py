@@ -37,14 +37,16 @@ class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("n_slices", ctypes.c_int),
                 ("a_en", ctypes.c_double), ("a_ee", ctypes.c_double),
                 ("x_components", ctypes.c_int), ("device_pointers", ctypes.c_int),
-                ("max_work_bytes", ctypes.c_size_t), ("stream", ctypes.c_void_p)]
+                ("max_work_bytes", ctypes.c_size_t), ("stream", ctypes.c_void_p),
+                ("pair_fp64", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [("ms_total", ctypes.c_double), ("ms_h2d", ctypes.c_double),
                 ("ms_pair", ctypes.c_double), ("ms_x", ctypes.c_double),
                 ("ms_int2e", ctypes.c_double), ("ms_d2h", ctypes.c_double),
-                ("n_r1_tiles", ctypes.c_int), ("gpu_launches", ctypes.c_int)]
+                ("n_r1_tiles", ctypes.c_int), ("gpu_launches", ctypes.c_int),
+                ("ms_x_gemm", ctypes.c_double), ("n_x_gemm", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -113,7 +115,7 @@ def cutc_int(nxBlocks, nyBlocks, nzBlocks, blockxSize, blockySize, blockzSize,
 
 
 def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_components=3,
-            device_pointers=False, max_work_bytes=0, stream=None) -> Options:
+            device_pointers=False, max_work_bytes=0, stream=None, pair_fp64=False) -> Options:
     o = Options()
     load().cutc_default_options(ctypes.byref(o))
     o.precision = precision
@@ -124,6 +126,7 @@ def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_component
     o.device_pointers = 1 if device_pointers else 0
     o.max_work_bytes = max_work_bytes
     o.stream = stream
+    o.pair_fp64 = 1 if pair_fp64 else 0
     return o
 
 
@@ -137,7 +140,7 @@ def cutc_int_ex(opt: Options, n_grid1, n_grid2, n_ao, n_nuc, size_bh,
 
 
 def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
-                    max_work_bytes=0, with_stats=False):
+                    max_work_bytes=0, with_stats=False, pair_fp64=False):
     """Host-array convenience call on a synth.Problem: returns (X, int_2e[, stats]).
 
     X is (x_components, n1, nA^2) == Fortran (nA, nA, n1, comps); int_2e is
@@ -146,7 +149,8 @@ def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
     X = np.empty((x_components, p.n_grid1, p.n_ao ** 2))
     I = np.empty((p.n_ao ** 2, p.n_ao ** 2))
     st = Stats()
-    opt = options(precision, n_slices, p.a_en, p.a_ee, x_components, False, max_work_bytes)
+    opt = options(precision, n_slices, p.a_en, p.a_ee, x_components, False, max_work_bytes,
+                  None, pair_fp64)
     s = cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
                     p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2,
                     p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I, st)

@@ -254,9 +254,31 @@ static size_t r1_row_bytes(const Request &R)
     return g;
 }
 
-int run_build(Engine *E, const Request &R, cutc_stats *stats)
+int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
 {
-    CUTC_TRY(validate(R));
+    CUTC_TRY(validate(R_in));
+    Request R = R_in;
+    // The term table is built on the host; with device pointers the Jastrow
+    // parameters are brought over first (they are tiny: size_bh x n_nuc).
+    std::vector<double> h_c;
+    std::vector<int> h_m, h_n, h_o;
+    if (R.device_pointers && R.nB > 0) {
+        const size_t nt_in = (size_t)R.nB * R.nN;
+        cudaStream_t s0 = R.stream ? R.stream : E->stream;
+        h_c.resize(nt_in);
+        h_m.resize(nt_in);
+        h_n.resize(nt_in);
+        h_o.resize(nt_in);
+        CUTC_CUDA_TRY(cudaMemcpyAsync(h_c.data(), R.c_bh, nt_in * 8, cudaMemcpyDeviceToHost, s0));
+        CUTC_CUDA_TRY(cudaMemcpyAsync(h_m.data(), R.m_bh, nt_in * 4, cudaMemcpyDeviceToHost, s0));
+        CUTC_CUDA_TRY(cudaMemcpyAsync(h_n.data(), R.n_bh, nt_in * 4, cudaMemcpyDeviceToHost, s0));
+        CUTC_CUDA_TRY(cudaMemcpyAsync(h_o.data(), R.o_bh, nt_in * 4, cudaMemcpyDeviceToHost, s0));
+        CUTC_CUDA_TRY(cudaStreamSynchronize(s0));
+        R.c_bh = h_c.data();
+        R.m_bh = h_m.data();
+        R.n_bh = h_n.data();
+        R.o_bh = h_o.data();
+    }
     std::vector<double> coef;
     std::vector<int> exps, off;
     CUTC_TRY(build_terms(R, coef, exps, off));
@@ -328,6 +350,14 @@ int run_build(Engine *E, const Request &R, cutc_stats *stats)
         n1t = std::min<int64_t>(n1t, R.tile_rows);
     const int n_tiles = (int)((n1 + n1t - 1) / n1t);
 
+    if (stats) {
+        while ((int)E->tile_ev.size() < 4 * n_tiles) {
+            cudaEvent_t e;
+            CUTC_CUDA_TRY(cudaEventCreate(&e));
+            E->tile_ev.push_back(e);
+        }
+    }
+
     // ---- per-point and pair-product terms -----------------------------------
     NucTerm *d_t1;
     double *d_f2, *d_P, *d_G, *d_Xp;
@@ -367,14 +397,15 @@ int run_build(Engine *E, const Request &R, cutc_stats *stats)
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[2], st));
 
     // ---- X build, tile by tile ------------------------------------------------
-    double ms_pair = 0.0;
     CUBLAS_TRY(cublasSetStream(E->blas, st));
     for (int tile = 0; tile < n_tiles; tile++) {
         const int i0 = (int)(tile * n1t);
         const int nb = (int)std::min<int64_t>(n1t, n1 - i0);
+        cudaEvent_t *tev = stats ? &E->tile_ev[4 * tile] : nullptr;
         CUTC_TRY(launch_r1_terms(st, i0, nb, nN, d_r1, d_rn, R.a_en, d_t1));
-        CUTC_CUDA_TRY(cudaEventRecord(E->ev[3], st));
-        if (R.precision == CUTC_PLAIN_FP64) {
+        if (tev)
+            CUTC_CUDA_TRY(cudaEventRecord(tev[0], st));
+        if (R.precision == CUTC_PLAIN_FP64 || R.pair_fp64) {
             PairArgs P;
             P.i0 = i0; P.n1b = nb; P.n2 = n2; P.nN = nN; P.n_terms = nt;
             P.r1 = d_r1; P.r2 = d_r2; P.t1 = d_t1; P.f2 = d_f2;
@@ -383,6 +414,11 @@ int run_build(Engine *E, const Request &R, cutc_stats *stats)
             P.G = d_G; P.ldg = n2; P.plane = (int64_t)nb * n2;
             CUTC_TRY(launch_pair_f64(st, P));
             note_launches(2);
+            if (R.precision == CUTC_SPLIT_BF16) {
+                // the split slicer reads (hi, lo) pairs: convert in place
+                CUTC_TRY(launch_f64_to_df(st, d_G, 4 * (int64_t)nb * n2));
+                note_launches(1);
+            }
         } else {
             PairDfArgs P;
             P.i0 = i0; P.n1b = nb; P.n2 = n2; P.nN = nN; P.rows_per_cta = 0;
@@ -396,20 +432,22 @@ int run_build(Engine *E, const Request &R, cutc_stats *stats)
             CUTC_TRY(launch_pair_df(st, P, pexp, d_rn, R.a_en));
             note_launches(3);
         }
-        CUTC_CUDA_TRY(cudaEventRecord(E->ev[4], st));
+        if (tev)
+            CUTC_CUDA_TRY(cudaEventRecord(tev[1], st));
         if (R.precision == CUTC_PLAIN_FP64) {
             // Xp[(m n1 + i0 + i) np + p] = sum_g P[p n2 + g] G[m plane + i n2 + g]
             const double one = 1.0, zero = 0.0;
+            if (tev)
+                CUTC_CUDA_TRY(cudaEventRecord(tev[2], st));
             CUBLAS_TRY(cublasDgemmStridedBatched(
                 E->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)np, nb, n2, &one, d_P, n2, 0, d_G, n2,
                 (long long)nb * n2, &zero, d_Xp + (int64_t)i0 * np, (int)np,
                 (long long)n1 * np, 4));
+            if (tev)
+                CUTC_CUDA_TRY(cudaEventRecord(tev[3], st));
         } else {
-            CUTC_TRY(split_x_tile(E, R, st, sp, reinterpret_cast<const float2 *>(d_G), i0, nb, d_Xp));
-        }
-        if (stats) {
-            CUTC_CUDA_TRY(cudaEventSynchronize(E->ev[4]));
-            ms_pair += ev_ms(E->ev[3], E->ev[4]);
+            CUTC_TRY(split_x_tile(E, R, st, sp, reinterpret_cast<const float2 *>(d_G), i0, nb, d_Xp,
+                                  tev ? tev[2] : nullptr, tev ? tev[3] : nullptr));
         }
     }
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[5], st));
@@ -457,6 +495,13 @@ int run_build(Engine *E, const Request &R, cutc_stats *stats)
     CUTC_CUDA_TRY(cudaGetLastError());
 
     if (stats) {
+        double ms_pair = 0.0, ms_gemm = 0.0;
+        for (int t = 0; t < n_tiles; t++) {
+            ms_pair += ev_ms(E->tile_ev[4 * t], E->tile_ev[4 * t + 1]);
+            ms_gemm += ev_ms(E->tile_ev[4 * t + 2], E->tile_ev[4 * t + 3]);
+        }
+        stats->ms_x_gemm = ms_gemm;
+        stats->n_x_gemm = n_tiles;
         stats->ms_h2d = ev_ms(E->ev[0], E->ev[1]);
         stats->ms_pair = ms_pair;
         stats->ms_x = ev_ms(E->ev[1], E->ev[5]) - ms_pair;
@@ -564,6 +609,7 @@ extern "C" int cutc_int_ex(const cutc_options *opt, int n_grid1, int n_grid2, in
     R.device_pointers = opt->device_pointers;
     R.max_work_bytes = opt->max_work_bytes;
     R.stream = (cudaStream_t)opt->stream;
+    R.pair_fp64 = opt->pair_fp64;
     R.n1 = n_grid1; R.n2 = n_grid2; R.nA = n_ao; R.nN = n_nuc; R.nB = size_bh;
     R.r1 = r1; R.wr1 = wr1; R.r2 = r2; R.wr2 = wr2; R.rn = rn;
     R.aos1 = aos_data1; R.aos2 = aos_data2;

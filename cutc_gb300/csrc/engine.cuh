@@ -32,6 +32,7 @@ struct Engine {
     cudaStream_t stream = nullptr;
     cublasHandle_t blas = nullptr;
     cudaEvent_t ev[kNumEvents];
+    std::vector<cudaEvent_t> tile_ev;  // per-tile timing events (grown on demand)
     Workspace ws;
     std::mutex mu;
 };
@@ -45,6 +46,7 @@ struct Request {
     int device_pointers = 0;
     size_t max_work_bytes = 0;
     int tile_rows = 0;  // optional cap on r1 rows per tile
+    int pair_fp64 = 0;  // split form: FP64 pair terms
     cudaStream_t stream = nullptr;
     int n1 = 0, n2 = 0, nA = 0, nN = 0, nB = 0;
     const double *r1 = nullptr, *wr1 = nullptr, *r2 = nullptr, *wr2 = nullptr, *rn = nullptr;

@@ -53,6 +53,8 @@ struct PairDfArgs {
 };
 
 int pair_df_max_exp(const int *exps, int n_terms);
+// in place: x[i] (FP64) -> (hi, lo) float pair at the same 8 bytes
+int launch_f64_to_df(cudaStream_t st, double *x, int64_t n);
 size_t pair_df_poly_bytes(int E, int n1b, int nN);
 int launch_r2_df(cudaStream_t st, int n2, int nN, const double *r2, const double *f2, float2 *r2d,
                  float2 *f2d);

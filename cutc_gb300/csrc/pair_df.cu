@@ -265,6 +265,22 @@ pair_df_kernel(PairDfArgs P)
     }
 }
 
+__global__ void f64_to_df_kernel(double *x, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const df::D v = df::from_double(x[i]);
+        reinterpret_cast<float2 *>(x)[i] = make_float2(v.hi, v.lo);
+    }
+}
+
+int launch_f64_to_df(cudaStream_t st, double *x, int64_t n)
+{
+    f64_to_df_kernel<<<4 * 152, 256, 0, st>>>(x, n);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    return CUTC_OK;
+}
+
 int pair_df_max_exp(const int *exps, int n_terms)
 {
     int E = 0;

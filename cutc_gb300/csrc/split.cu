@@ -745,7 +745,7 @@ int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *
 }
 
 int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const float2 *G,
-                 int i0, int nb, double *Xp)
+                 int i0, int nb, double *Xp, cudaEvent_t gemm_begin, cudaEvent_t gemm_end)
 {
     (void)E;
     SplitPlan &S_ = sp;
@@ -756,7 +756,11 @@ int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, co
     SrcDenseDF src{G, (int64_t)R.n2};
     CUTC_SLICES_DISPATCH(sp.n_slices, {
         CUTC_TRY((slice_rows<S, SrcDenseDF>(st, src, B)));
+        if (gemm_begin)
+            CUTC_CUDA_TRY(cudaEventRecord(gemm_begin, st));
         CUTC_TRY((gemm<S>(st, S_.AX, B, 1.0, Xp, np, nb, R.n1, i0, 0, S_.err)));
+        if (gemm_end)
+            CUTC_CUDA_TRY(cudaEventRecord(gemm_end, st));
     });
     return CUTC_OK;
 }

@@ -36,7 +36,7 @@ int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *
                     const double *aos2v, int64_t n1t, int slot0, SplitPlan &sp);
 // G is the df tile G[c][i][j] as (hi, lo) float pairs
 int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const float2 *G,
-                 int i0, int nb, double *Xp);
+                 int i0, int nb, double *Xp, cudaEvent_t gemm_begin, cudaEvent_t gemm_end);
 int split_int2e(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const double *wr1,
                 const double *aos1, const double *Xp, double *I);
 // C[m + ldc n] = sum_k A[m K + k] B[n K + k] through the split form (device arrays)

@@ -65,6 +65,7 @@ typedef struct cutc_options {
     int device_pointers;    /* 1: every array argument is a device pointer */
     size_t max_work_bytes;  /* device budget for the r1 tiles; 0 = automatic */
     void *stream;           /* cudaStream_t to run on; NULL = the engine's stream */
+    int pair_fp64;          /* split form: 1 = pair terms in FP64 instead of double-float */
 } cutc_options;
 
 typedef struct cutc_stats {
@@ -76,6 +77,8 @@ typedef struct cutc_stats {
     double ms_d2h;          /* device -> host copies */
     int n_r1_tiles;         /* r1 tiles the X build was split into */
     int gpu_launches;       /* kernels of this library launched by the call */
+    double ms_x_gemm;       /* device time of the X-build contraction launches alone */
+    int n_x_gemm;           /* number of those launches (one per r1 tile) */
 } cutc_stats;
 
 /* Fills the defaults: plain FP64, 5 slices, a_en = a_ee = 1, 3 X components. */
