@@ -38,7 +38,7 @@ class Options(ctypes.Structure):
                 ("a_en", ctypes.c_double), ("a_ee", ctypes.c_double),
                 ("x_components", ctypes.c_int), ("device_pointers", ctypes.c_int),
                 ("max_work_bytes", ctypes.c_size_t), ("stream", ctypes.c_void_p),
-                ("pair_fp64", ctypes.c_int)]
+                ("pair_fp64", ctypes.c_int), ("k_split", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -115,7 +115,8 @@ def cutc_int(nxBlocks, nyBlocks, nzBlocks, blockxSize, blockySize, blockzSize,
 
 
 def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_components=3,
-            device_pointers=False, max_work_bytes=0, stream=None, pair_fp64=False) -> Options:
+            device_pointers=False, max_work_bytes=0, stream=None, pair_fp64=False,
+            k_split=0) -> Options:
     o = Options()
     load().cutc_default_options(ctypes.byref(o))
     o.precision = precision
@@ -127,6 +128,7 @@ def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_component
     o.max_work_bytes = max_work_bytes
     o.stream = stream
     o.pair_fp64 = 1 if pair_fp64 else 0
+    o.k_split = k_split
     return o
 
 
@@ -140,7 +142,7 @@ def cutc_int_ex(opt: Options, n_grid1, n_grid2, n_ao, n_nuc, size_bh,
 
 
 def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
-                    max_work_bytes=0, with_stats=False, pair_fp64=False):
+                    max_work_bytes=0, with_stats=False, pair_fp64=False, k_split=0):
     """Host-array convenience call on a synth.Problem: returns (X, int_2e[, stats]).
 
     X is (x_components, n1, nA^2) == Fortran (nA, nA, n1, comps); int_2e is
@@ -150,7 +152,7 @@ def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
     I = np.empty((p.n_ao ** 2, p.n_ao ** 2))
     st = Stats()
     opt = options(precision, n_slices, p.a_en, p.a_ee, x_components, False, max_work_bytes,
-                  None, pair_fp64)
+                  None, pair_fp64, k_split)
     s = cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
                     p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2,
                     p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I, st)

@@ -220,6 +220,10 @@ static int validate(const Request &R)
         cutc_set_error(CUTC_ERR_INVALID, "unknown precision form %d", R.precision);
         return CUTC_ERR_INVALID;
     }
+    if (R.k_split < 0 || (R.k_split > 0 && R.k_split < 64)) {
+        cutc_set_error(CUTC_ERR_INVALID, "k_split must be 0 or at least 64");
+        return CUTC_ERR_INVALID;
+    }
     if (R.precision == CUTC_SPLIT_BF16 && (R.n_slices < 3 || R.n_slices > kMaxSlices)) {
         cutc_set_error(CUTC_ERR_INVALID, "n_slices must be in [3, %d]", kMaxSlices);
         return CUTC_ERR_INVALID;
@@ -610,6 +614,7 @@ extern "C" int cutc_int_ex(const cutc_options *opt, int n_grid1, int n_grid2, in
     R.max_work_bytes = opt->max_work_bytes;
     R.stream = (cudaStream_t)opt->stream;
     R.pair_fp64 = opt->pair_fp64;
+    R.k_split = opt->k_split;
     R.n1 = n_grid1; R.n2 = n_grid2; R.nA = n_ao; R.nN = n_nuc; R.nB = size_bh;
     R.r1 = r1; R.wr1 = wr1; R.r2 = r2; R.wr2 = wr2; R.rn = rn;
     R.aos1 = aos_data1; R.aos2 = aos_data2;

@@ -47,6 +47,7 @@ struct Request {
     size_t max_work_bytes = 0;
     int tile_rows = 0;  // optional cap on r1 rows per tile
     int pair_fp64 = 0;  // split form: FP64 pair terms
+    int k_split = 0;    // split form: max K per tensor-core launch (0 = default)
     cudaStream_t stream = nullptr;
     int n1 = 0, n2 = 0, nA = 0, nN = 0, nB = 0;
     const double *r1 = nullptr, *wr1 = nullptr, *r2 = nullptr, *wr2 = nullptr, *rn = nullptr;

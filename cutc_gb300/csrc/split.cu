@@ -9,16 +9,22 @@
 //     A[r, k] = 2^{e_r} sum_{s < S} a_s[r, k],  a_s = q_s 2^{-8-9s},  q_s in [-256, 256]
 // (S signed 9-bit digits of the row-scaled value, rounded at the last digit:
 // relative error <= 2^{-9S}), and every digit is an exact BF16 number.  The
-// products a_s b_t with s + t <= S - 1 run as tcgen05.mma kind::f16 (BF16 in,
-// FP32 accumulate in tensor memory), one accumulator per diagonal d = s + t:
+// products a_s b_t with s + t <= D = S - 1 run as tcgen05.mma kind::f16 (BF16
+// in, FP32 accumulate in tensor memory), one accumulator per diagonal d = s + t:
+//   * the accumulator of diagonal d sits at tensor-memory column BN d, so the
+//     products of slice a_s with b_0 .. b_{D-s} -- the B slices stacked in
+//     shared memory -- are ONE instruction of width N = BN (D + 1 - s) that
+//     lands on diagonals s .. D: S instructions per 16-wide K step instead of
+//     S (S + 1) / 2, and A is read from shared memory once per slice, which
+//     keeps the operand traffic under the shared-memory bandwidth;
 //   * every product of diagonal d is an integer multiple of 2^{-16-9d} of
 //     magnitude <= 2^{-9d}, so the FP32 accumulator holds the exact sum while
-//     (d + 1) * Kc * 2^16 < 2^24; with the chunk Kc = 64 this holds for d <= 2;
-//   * after each chunk the d = 0 and d = 1 sums are added error-free into
-//     FP32 (hi, lo) register pairs (hi on a coarse grid, lo the remainder),
-//     d = 2 is added into an FP32 running sum kept in tensor memory, and the
-//     small diagonals d >= 3 stay in one tensor-memory accumulator for the
-//     whole K range;
+//     (d + 1) * Kc * 2^16 <= 2^24; with the chunk Kc = 64 this holds for d <= 3;
+//   * after each chunk the epilogue adds the d = 0, 1, 2 sums error-free into
+//     FP32 (hi, lo) register pairs (hi on a coarse grid, lo the remainder)
+//     and d >= 3 (relative size 2^-27) into a plain FP32 sum; nothing is
+//     carried across chunks in tensor memory, whose FP32 accumulation
+//     rounding would otherwise grow with K;
 //   * the accumulators are double-buffered in tensor memory, so the flush of
 //     chunk c overlaps the MMAs of chunk c + 1;
 //   * at the end the pieces are summed in FP64 and scaled by alpha 2^{e_r + f_n}.
@@ -45,19 +51,15 @@ namespace cutc {
 // ---------------------------------------------------------------------------
 
 constexpr int kBM = 128;        // rows of A per CTA (TMEM lanes)
-constexpr int kBN = 64;         // rows of B (output columns) per CTA
 constexpr int kBK = 32;         // K per TMA box: 32 BF16 = 64-byte rows (64B swizzle)
 constexpr int kChunkBlocks = 2; // exact-accumulation chunk: 64 K
-constexpr int kEpiWarps = 16;   // 4 lane quarters x 4 column groups of 16
-constexpr int kTmaWarp = kEpiWarps;
-constexpr int kMmaWarp = kEpiWarps + 1;
-constexpr int kGemmThreads = (kEpiWarps + 2) * 32;
 constexpr int kMaxKPerLaunch = 1 << 18;  // keeps every exact (hi, lo) sum below 2^24 units
 constexpr uint32_t kTmemCols = 512;
-// tensor-memory columns: buffer b holds diagonals 0, 1, 2 at 192 b + 64 d; d >= 3 at 384;
-// the epilogue keeps its running FP32 sum of diagonal 2 at 448
-constexpr uint32_t kAcc3Col = 384;
-constexpr uint32_t kSum2Col = 448;
+constexpr int kGroupM = 8;      // row tiles per raster group (A tiles shared through L2)
+
+// Output-column tile for S slices: S diagonals x 2 buffers must fit 512 columns
+// and the widest instruction (N = BN S) must not exceed 256.
+__host__ __device__ constexpr int bn_for(int S) { return S <= 5 ? 48 : 32; }
 
 struct GemmParams {
     int M, N;
@@ -77,13 +79,24 @@ struct GemmParams {
 
 template <int S>
 struct GemmCfg {
+    static constexpr int kBN = bn_for(S);
+    static constexpr int kCW = 8;                    // columns per epilogue warp
+    static constexpr int kEpiWarps = 4 * (kBN / kCW); // 4 lane quarters x column groups
+    static constexpr int kTmaWarp = kEpiWarps;
+    static constexpr int kMmaWarp = kEpiWarps + 1;
+    static constexpr int kThreads = (kEpiWarps + 2) * 32;
+    static constexpr int kBuf = kBN * S;             // tensor-memory columns per buffer
     static constexpr int kASlice = kBM * kBK * 2;
     static constexpr int kBSlice = kBN * kBK * 2;
     static constexpr int kStage = S * (kASlice + kBSlice);
-    static constexpr int kStages = (200 * 1024) / kStage < 4 ? (200 * 1024) / kStage : 4;
+    static constexpr int kStagesFit = (220 * 1024) / kStage;
+    static constexpr int kStages = kStagesFit < 4 ? kStagesFit : 4;
     static constexpr int kBarBytes = 256;
     static constexpr int kSmem = kStages * kStage + 1024 + kBarBytes;
     static_assert(kStages >= 2, "not enough shared memory for two stages");
+    static_assert(2 * kBuf <= (int)kTmemCols, "accumulators exceed tensor memory");
+    static_assert(kBN * S <= 256, "instruction N exceeds 256");
+    static_assert(kBSlice % 512 == 0, "B slices must stack on 8-row swizzle atoms");
 };
 
 __device__ __forceinline__ double pow2(int e)
@@ -93,12 +106,14 @@ __device__ __forceinline__ double pow2(int e)
 }
 
 template <int S>
-__global__ void __launch_bounds__(kGemmThreads, 1)
+__global__ void __launch_bounds__(GemmCfg<S>::kThreads, 1)
 split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   GemmParams P)
 {
     using Cfg = GemmCfg<S>;
     constexpr int D = S - 1;  // highest diagonal kept
+    constexpr int BN = Cfg::kBN, CW = Cfg::kCW;
+    constexpr int kEpiWarps = Cfg::kEpiWarps, kTmaWarp = Cfg::kTmaWarp, kMmaWarp = Cfg::kMmaWarp;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -112,7 +127,14 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     volatile int *s_abort = reinterpret_cast<volatile int *>(s_tmem + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+    // grouped raster: kGroupM row tiles share the A tiles through L2
+    const int num_m = P.Mpad / kBM, num_n = P.Npad / BN;
+    const int per_group = kGroupM * num_n;
+    const int tid = blockIdx.x;
+    const int gfirst = (tid / per_group) * kGroupM;
+    const int gsize = min(num_m - gfirst, kGroupM);
+    const int m0 = (gfirst + (tid % per_group) % gsize) * kBM;
+    const int n0 = ((tid % per_group) / gsize) * BN;
     const int nkb = P.nkb;
     const int nch = (nkb + kChunkBlocks - 1) / kChunkBlocks;
 
@@ -179,8 +201,6 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         }
     } else if (warp == kMmaWarp) {
         if (lane == 0) {
-            constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
-            bool acc3_init = false;
             bool ok = true;
             for (int c = 0; c < nch && ok; c++) {
                 const int b = c & 1;
@@ -189,7 +209,7 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                     break;
                 }
                 tc::fence_after_sync();
-                bool init[3] = {false, false, false};
+                bool first = true;
                 const int kb_end = min(nkb, (c + 1) * kChunkBlocks);
                 for (int kb = c * kChunkBlocks; kb < kb_end; kb++) {
                     const int stage = kb % Cfg::kStages, round = kb / Cfg::kStages;
@@ -202,25 +222,16 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                     const uint32_t sa = tc::smem_u32(smem + stage * Cfg::kStage);
                     const uint32_t sb = sa + S * Cfg::kASlice;
 #pragma unroll
-                    for (int s = 0; s < S; s++) {
+                    for (int k16 = 0; k16 < kBK / 16; k16++) {
+                        const uint64_t bd = tc::smem_desc_sw64(sb + k16 * 32);
 #pragma unroll
-                        for (int t = 0; t + s <= D; t++) {
-                            const int d = s + t;
-                            const uint32_t col = d < 3 ? 192u * b + 64u * d : kAcc3Col;
-#pragma unroll
-                            for (int k16 = 0; k16 < kBK / 16; k16++) {
-                                const uint64_t ad = tc::smem_desc_sw64(sa + s * Cfg::kASlice + k16 * 32);
-                                const uint64_t bd = tc::smem_desc_sw64(sb + t * Cfg::kBSlice + k16 * 32);
-                                uint32_t acc;
-                                if (d < 3) {
-                                    acc = init[d] ? 1u : 0u;
-                                    init[d] = true;
-                                } else {
-                                    acc = acc3_init ? 1u : 0u;
-                                    acc3_init = true;
-                                }
-                                tc::mma_bf16(tbase + col, ad, bd, idesc, acc);
-                            }
+                        for (int s = 0; s < S; s++) {
+                            // a_s x [b_0 .. b_{D-s}] -> diagonals s .. D
+                            const uint32_t idesc = tc::idesc_bf16_f32(kBM, BN * (D + 1 - s));
+                            const uint64_t ad = tc::smem_desc_sw64(sa + s * Cfg::kASlice + k16 * 32);
+                            tc::mma_bf16(tbase + (uint32_t)(Cfg::kBuf * b + BN * s), ad, bd, idesc,
+                                         first ? 0u : 1u);
+                            first = false;
                         }
                     }
                     tc::mma_commit(tc::smem_u32(&empty[stage]));
@@ -237,13 +248,15 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         // ---- epilogue: exact chunk flushes, then FP64 recombination ----------
         const int q = warp & 3, cgrp = warp >> 2;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        const uint32_t coff = 16u * cgrp;
-        float hi0[16], lo0[16], hi1[16], lo1[16];
+        const uint32_t coff = (uint32_t)(CW * cgrp);
+        float hi0[CW], lo0[CW], hi1[CW], lo1[CW], hi2[CW], lo2[CW], s3[CW];
 #pragma unroll
-        for (int j = 0; j < 16; j++)
-            hi0[j] = lo0[j] = hi1[j] = lo1[j] = 0.f;
-        const float C0 = 786432.0f;  // 1.5 * 2^19: rounds to multiples of 2^-4
-        const float C1 = 1536.0f;    // 1.5 * 2^10: rounds to multiples of 2^-13
+        for (int j = 0; j < CW; j++)
+            hi0[j] = lo0[j] = hi1[j] = lo1[j] = hi2[j] = lo2[j] = s3[j] = 0.f;
+        // v + C - C rounds v to the grid of C's binade: C = 1.5 2^(23 + g) gives multiples of 2^g
+        const float C0 = 786432.0f;  // 1.5 * 2^19: multiples of 2^-4  (d = 0, LSB 2^-16)
+        const float C1 = 1536.0f;    // 1.5 * 2^10: multiples of 2^-13 (d = 1, LSB 2^-25)
+        const float C2 = 3.0f;       // 1.5 * 2^1:  multiples of 2^-22 (d = 2, LSB 2^-34)
         bool ok = true;
         for (int c = 0; c < nch; c++) {
             const int b = c & 1;
@@ -254,36 +267,41 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             }
             tc::fence_after_sync();
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                float v[8];
-                const uint32_t cb = tbase + lane_off + 192u * b + coff + 8u * h;
-                tc::tmem_ld8(cb, v);
+            for (int h = 0; h < CW / 4; h++) {
+                const uint32_t cb = tbase + lane_off + (uint32_t)(Cfg::kBuf * b) + coff + 4u * h;
+                float v[4];
+                tc::tmem_ld4(cb, v);
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
+                for (int j = 0; j < 4; j++) {
                     const float x = v[j];
                     const float hh = __fsub_rn(__fadd_rn(x, C0), C0);
-                    hi0[8 * h + j] = __fadd_rn(hi0[8 * h + j], hh);
-                    lo0[8 * h + j] = __fadd_rn(lo0[8 * h + j], __fsub_rn(x, hh));
+                    hi0[4 * h + j] = __fadd_rn(hi0[4 * h + j], hh);
+                    lo0[4 * h + j] = __fadd_rn(lo0[4 * h + j], __fsub_rn(x, hh));
                 }
-                tc::tmem_ld8(cb + 64u, v);
+                tc::tmem_ld4(cb + BN, v);
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
+                for (int j = 0; j < 4; j++) {
                     const float x = v[j];
                     const float hh = __fsub_rn(__fadd_rn(x, C1), C1);
-                    hi1[8 * h + j] = __fadd_rn(hi1[8 * h + j], hh);
-                    lo1[8 * h + j] = __fadd_rn(lo1[8 * h + j], __fsub_rn(x, hh));
+                    hi1[4 * h + j] = __fadd_rn(hi1[4 * h + j], hh);
+                    lo1[4 * h + j] = __fadd_rn(lo1[4 * h + j], __fsub_rn(x, hh));
                 }
                 if (D >= 2) {
-                    const uint32_t sum2 = tbase + lane_off + kSum2Col + coff + 8u * h;
-                    tc::tmem_ld8(cb + 128u, v);
-                    if (c > 0) {
-                        float a2[8];
-                        tc::tmem_ld8(sum2, a2);
+                    tc::tmem_ld4(cb + 2 * BN, v);
 #pragma unroll
-                        for (int j = 0; j < 8; j++)
-                            v[j] = __fadd_rn(a2[j], v[j]);
+                    for (int j = 0; j < 4; j++) {
+                        const float x = v[j];
+                        const float hh = __fsub_rn(__fadd_rn(x, C2), C2);
+                        hi2[4 * h + j] = __fadd_rn(hi2[4 * h + j], hh);
+                        lo2[4 * h + j] = __fadd_rn(lo2[4 * h + j], __fsub_rn(x, hh));
                     }
-                    tc::tmem_st8(sum2, v);
+                }
+#pragma unroll
+                for (int d = 3; d <= D; d++) {
+                    tc::tmem_ld4(cb + d * BN, v);
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        s3[4 * h + j] = __fadd_rn(s3[4 * h + j], v[j]);
                 }
             }
             tc::fence_before_sync();
@@ -292,32 +310,20 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                 tc::mbar_arrive(tc::smem_u32(&tempty[b]));
         }
         const int m = m0 + q * 32 + lane;
-        const int em = (ok && m < P.M) ? P.ea[m] : 0;
+        if (ok && m < P.M) {
+            const int em = P.ea[m];
 #pragma unroll
-        for (int h = 0; h < 4; h++) {
-            float v3[4], a2[4];
-#pragma unroll
-            for (int j = 0; j < 4; j++)
-                v3[j] = a2[j] = 0.f;
-            if (ok && D >= 3)
-                tc::tmem_ld4(tbase + lane_off + kAcc3Col + coff + 4u * h, v3);
-            if (ok && D >= 2 && nch > 0)
-                tc::tmem_ld4(tbase + lane_off + kSum2Col + coff + 4u * h, a2);
-            if (ok && m < P.M) {
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const int jj = 4 * h + j;
-                    const int n = n0 + (int)coff + jj;
-                    if (n < P.N) {
-                        double val = ((double)hi0[jj] + (double)hi1[jj]) +
-                                     (((double)lo0[jj] + (double)lo1[jj]) +
-                                      ((double)a2[j] + (double)v3[j]));
-                        val *= P.alpha * pow2(em + P.eb[n]);
-                        const int64_t col = (int64_t)(n / P.ncol_group) * P.group_stride +
-                                            P.col0 + n % P.ncol_group;
-                        double *dst = P.C + m + P.ldc * col;
-                        *dst = P.accumulate ? *dst + val : val;
-                    }
+            for (int j = 0; j < CW; j++) {
+                const int n = n0 + (int)coff + j;
+                if (n < P.N) {
+                    double val = (((double)hi0[j] + (double)hi1[j]) +
+                                  ((double)hi2[j] + (double)lo0[j])) +
+                                 (((double)lo1[j] + (double)lo2[j]) + (double)s3[j]);
+                    val *= P.alpha * pow2(em + P.eb[n]);
+                    const int64_t col = (int64_t)(n / P.ncol_group) * P.group_stride + P.col0 +
+                                        n % P.ncol_group;
+                    double *dst = P.C + m + P.ldc * col;
+                    *dst = P.accumulate ? *dst + val : val;
                 }
             }
         }
@@ -635,7 +641,7 @@ static int slice_cols(cudaStream_t st, const double *X, int64_t ld, int64_t k0, 
 template <int S>
 static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alpha, double *C,
                 int64_t ldc, int ncol_group, int64_t group_stride, int64_t col0, int accumulate,
-                int *err)
+                int *err, int k_split = 0)
 {
     using Cfg = GemmCfg<S>;
     static bool attr = false;
@@ -646,14 +652,15 @@ static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alph
     }
     CUtensorMap ta, tb;
     CUTC_TRY(make_tmap(&ta, A.sl, (int64_t)S * A.Mpad, A.Kpad, kBM));
-    CUTC_TRY(make_tmap(&tb, B.sl, (int64_t)S * B.Mpad, B.Kpad, kBN));
+    CUTC_TRY(make_tmap(&tb, B.sl, (int64_t)S * B.Mpad, B.Kpad, Cfg::kBN));
     const int nkb_total = (int)(A.Kpad / kBK);
-    const int kb_per = kMaxKPerLaunch / kBK;
-    dim3 grid(A.Mpad / kBM, B.Mpad / kBN);
-    if (grid.y > 65535) {
-        cutc_set_error(CUTC_ERR_INVALID, "GEMM N extent too large (%d tiles)", (int)grid.y);
+    const int kmax = (k_split > 0 && k_split < kMaxKPerLaunch) ? k_split : kMaxKPerLaunch;
+    const int kb_per = std::max(1, kmax / kBK);
+    if (A.Mpad % kBM || B.Mpad % Cfg::kBN) {
+        cutc_set_error(CUTC_ERR_INVALID, "operand padding does not match the tile");
         return CUTC_ERR_INVALID;
     }
+    dim3 grid((unsigned)((int64_t)(A.Mpad / kBM) * (B.Mpad / Cfg::kBN)));
     for (int kb0 = 0; kb0 < nkb_total; kb0 += kb_per) {
         GemmParams P;
         P.M = A.M;
@@ -672,7 +679,7 @@ static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alph
         P.col0 = col0;
         P.accumulate = (accumulate || kb0 > 0) ? 1 : 0;
         P.err = err;
-        split_gemm_kernel<S><<<grid, kGemmThreads, Cfg::kSmem, st>>>(ta, tb, P);
+        split_gemm_kernel<S><<<grid, Cfg::kThreads, Cfg::kSmem, st>>>(ta, tb, P);
         CUTC_CUDA_TRY(cudaGetLastError());
         note_launches(1);
     }
@@ -738,7 +745,8 @@ int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *
     CUTC_TRY(upload_pairs(W, slot0 + SS_PAIRS_SYM, st, R.nA, false, &S_.pairs_sym));
     CUTC_TRY(upload_pairs(W, slot0 + SS_PAIRS_ANTI, st, R.nA, true, &S_.pairs_anti));
     CUTC_TRY(alloc_operand(W, slot0 + SS_AX, R.n_slices, np, kBM, R.n2, S_.AX));
-    CUTC_TRY(alloc_operand(W, slot0 + SS_BX, R.n_slices, (int)(4 * n1t), kBN, R.n2, S_.BX));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BX, R.n_slices, (int)(4 * n1t), bn_for(R.n_slices), R.n2,
+                           S_.BX));
     SrcSym src{wr2, aos2v, (int64_t)R.n2, S_.pairs_sym};
     CUTC_SLICES_DISPATCH(R.n_slices, CUTC_TRY((slice_rows<S, SrcSym>(st, src, S_.AX))));
     return CUTC_OK;
@@ -751,14 +759,14 @@ int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, co
     SplitPlan &S_ = sp;
     Operand B = S_.BX;
     B.M = 4 * nb;  // rows (c, i) of this tile; Mpad keeps the allocated padding
-    B.Mpad = (int)round_up(B.M, kBN);
+    B.Mpad = (int)round_up(B.M, bn_for(sp.n_slices));
     const int64_t np = n_pairs(R.nA);
     SrcDenseDF src{G, (int64_t)R.n2};
     CUTC_SLICES_DISPATCH(sp.n_slices, {
         CUTC_TRY((slice_rows<S, SrcDenseDF>(st, src, B)));
         if (gemm_begin)
             CUTC_CUDA_TRY(cudaEventRecord(gemm_begin, st));
-        CUTC_TRY((gemm<S>(st, S_.AX, B, 1.0, Xp, np, nb, R.n1, i0, 0, S_.err)));
+        CUTC_TRY((gemm<S>(st, S_.AX, B, 1.0, Xp, np, nb, R.n1, i0, 0, S_.err, R.k_split)));
         if (gemm_end)
             CUTC_CUDA_TRY(cudaEventRecord(gemm_end, st));
     });
@@ -776,8 +784,9 @@ int split_int2e(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, con
     Operand AH, AN, BH, BN;
     CUTC_TRY(alloc_operand(W, slot0 + SS_AH, sp.n_slices, np, kBM, n1, AH));
     CUTC_TRY(alloc_operand(W, slot0 + SS_AN, sp.n_slices, np, kBM, 3 * (int64_t)n1, AN));
-    CUTC_TRY(alloc_operand(W, slot0 + SS_BH, sp.n_slices, np, kBN, n1, BH));
-    CUTC_TRY(alloc_operand(W, slot0 + SS_BN, sp.n_slices, std::max(nl, 1), kBN, 3 * (int64_t)n1, BN));
+    const int bn = bn_for(sp.n_slices);
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BH, sp.n_slices, np, bn, n1, BH));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BN, sp.n_slices, std::max(nl, 1), bn, 3 * (int64_t)n1, BN));
     BN.M = nl;
     void *p;
     CUTC_TRY(W.get(slot0 + SS_H, (size_t)np * np * 8, &p));
@@ -790,10 +799,10 @@ int split_int2e(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, con
         CUTC_TRY(slice_cols<S>(st, Xp, np, 3 * (int64_t)n1, AH));
         CUTC_TRY(slice_cols<S>(st, Xp, np, 0, AN));
         CUTC_TRY((slice_rows<S, SrcSym>(st, s0, BH)));
-        CUTC_TRY(gemm<S>(st, AH, BH, 1.0, H, np, np, 0, 0, 0, S_.err));
+        CUTC_TRY(gemm<S>(st, AH, BH, 1.0, H, np, np, 0, 0, 0, S_.err, R.k_split));
         if (nl > 0) {
             CUTC_TRY((slice_rows<S, SrcAnti>(st, sa, BN)));
-            CUTC_TRY(gemm<S>(st, AN, BN, -0.5, N, np, nl, 0, 0, 0, S_.err));
+            CUTC_TRY(gemm<S>(st, AN, BN, -0.5, N, np, nl, 0, 0, 0, S_.err, R.k_split));
         }
     });
     CUTC_TRY(launch_assemble_int2e(st, nA, H, N, I));
@@ -816,7 +825,7 @@ int split_gemm_dense(Engine *E, cudaStream_t st, int n_slices, int M, int N, int
     const int base = 200;
     Operand OA, OB;
     CUTC_TRY(alloc_operand(W, base, n_slices, M, kBM, K, OA));
-    CUTC_TRY(alloc_operand(W, base + 3, n_slices, N, kBN, K, OB));
+    CUTC_TRY(alloc_operand(W, base + 3, n_slices, N, bn_for(n_slices), K, OB));
     void *p;
     CUTC_TRY(W.get(base + 6, 64, &p));
     int *err = (int *)p;

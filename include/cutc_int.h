@@ -66,6 +66,8 @@ typedef struct cutc_options {
     size_t max_work_bytes;  /* device budget for the r1 tiles; 0 = automatic */
     void *stream;           /* cudaStream_t to run on; NULL = the engine's stream */
     int pair_fp64;          /* split form: 1 = pair terms in FP64 instead of double-float */
+    int k_split;            /* split form: max K per tensor-core launch; the partial results
+                               are summed in FP64 (0 = 262144) */
 } cutc_options;
 
 typedef struct cutc_stats {
