@@ -190,6 +190,20 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4])
         v[i] = __uint_as_float(r[i]);
 }
 
+// 32 lanes x 4 columns without waiting: the caller issues several and then
+// calls tmem_wait_ld() once before reading any of the values.
+__device__ __forceinline__ void tmem_ld4_nowait(uint32_t taddr, uint32_t (&r)[4])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld()
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 // Stores 8 consecutive columns of this warp's 32 lanes and waits for completion.
 __device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8])
 {
