@@ -30,7 +30,8 @@ SPLIT_BF16 = 1
 
 # every symbol include/cutc_int.h declares
 EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_default_options", "cutc_jast_bh_dev",
-           "cutc_split_gemm_dev", "cutc_validate_launch_dims", "cutc_last_error", "cutc_release"]
+           "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_validate_launch_dims",
+           "cutc_last_error", "cutc_release"]
 
 
 class Options(ctypes.Structure):
@@ -79,6 +80,8 @@ def load(path: str = LIB_PATH):
     L.cutc_default_options.restype = None
     L.cutc_jast_bh_dev.argtypes = [i] * 6 + [vp] * 7 + [dp, dp, vp]
     L.cutc_jast_bh_dev.restype = i
+    L.cutc_jast_bh_dev_noalloc.argtypes = [i] * 6 + [vp] * 7 + [dp, dp, vp, vp]
+    L.cutc_jast_bh_dev_noalloc.restype = i
     L.cutc_split_gemm_dev.argtypes = [i, i, i, ctypes.c_longlong, vp, vp, vp, ctypes.c_longlong]
     L.cutc_split_gemm_dev.restype = i
     L.cutc_validate_launch_dims.argtypes = [i] * 6
@@ -170,6 +173,22 @@ def jast_bh_device(r1, r2, rn, c_bh, m_bh, n_bh, o_bh, G, i0=0, n1b=None,
     return L.cutc_jast_bh_dev(i0, n1b, n1, r2.shape[0], rn.shape[0], c_bh.shape[1],
                               _vp(r1), _vp(r2), _vp(rn), _vp(c_bh), _vp(m_bh), _vp(n_bh),
                               _vp(o_bh), a_en, a_ee, _vp(G))
+
+
+def jast_bh_device_noalloc(r1, r2, rn, c_bh, m_bh, n_bh, o_bh, G, i0=0, n1b=None,
+                           a_en=1.0, a_ee=1.0, stream=None) -> int:
+    """Pair terms on device tensors through the allocation-free entry point.
+
+    Same results as jast_bh_device; its scratch is a fixed 32 MiB device array
+    inside the library, so the call allocates nothing.  Calls that overlap on
+    the GPU share that array and race.
+    """
+    n1 = r1.shape[0]
+    n1b = n1 - i0 if n1b is None else n1b
+    L = load()
+    return L.cutc_jast_bh_dev_noalloc(i0, n1b, n1, r2.shape[0], rn.shape[0], c_bh.shape[1],
+                                      _vp(r1), _vp(r2), _vp(rn), _vp(c_bh), _vp(m_bh), _vp(n_bh),
+                                      _vp(o_bh), a_en, a_ee, _vp(G), stream)
 
 
 def split_gemm_device(A, B, C=None, n_slices=5):

@@ -57,4 +57,7 @@ inline int64_t n_strict_pairs(int n) { return (int64_t)n * (n - 1) / 2; }
 
 inline unsigned ceil_div(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
 
+// Counts kernel launches of this library (reported in cutc_stats).
+void note_launches(int n);
+
 }  // namespace cutc

@@ -22,6 +22,9 @@
 //     reference's stride-n2 stores.
 // Terms with |c| < 1e-10 are dropped on the host (src/jast_bh.cu:203) and the
 // coalescence guard r^2 > 1e-15 (src/jast_bh.cu:143,169,189) is kept.
+#include <algorithm>
+#include <mutex>
+
 #include "common.cuh"
 #include "pair.cuh"
 
@@ -236,3 +239,157 @@ int launch_pair_f64(cudaStream_t st, const PairArgs &P)
 }
 
 }  // namespace cutc
+
+// ---------------------------------------------------------------------------
+// Allocation-free pair terms
+//
+// Some callers cannot let a library allocate device memory: code that is
+// being captured into a CUDA graph or runs inside a latency-critical serving
+// loop (cudaMalloc / cudaFree synchronise the device and are not allowed
+// during capture), and host programs whose own memory manager owns the whole
+// device.  cutc_jast_bh_dev_noalloc serves them: its scratch (the per-point
+// nucleus terms, the r2 e-n terms and the compact Jastrow term table) lives
+// in the static array below, sized once at load time, so a call allocates
+// nothing -- no cudaMalloc, no cudaFree, no library allocator, no engine
+// context.  The caller still provides the inputs and the output.
+// ---------------------------------------------------------------------------
+
+namespace cutc {
+
+// Fixed capacity of the scratch: every GPU that loads the library holds it until exit.
+constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// layout of the scratch
+constexpr size_t kNaStatus = 0;                                       // int status word
+constexpr size_t kNaCoef = 256;                                       // double[3 * kMaxTerms]
+constexpr size_t kNaExps = kNaCoef + 3 * sizeof(double) * kMaxTerms;  // int[kMaxTerms]
+constexpr size_t kNaOff = kNaExps + sizeof(int) * kMaxTerms;          // int[kMaxNuc + 1]
+constexpr size_t kNaT1 = (kNaOff + sizeof(int) * (kMaxNuc + 1) + 255) & ~(size_t)255;
+
+// The compact term table built on the device (the same table build_terms makes
+// on the host for the allocating entry points): terms with |c| < 1e-10 are
+// dropped (src/jast_bh.cu:203); an exponent outside [0, 6] sets the status.
+__global__ void noalloc_terms_kernel(int nN, int nB, const double *__restrict__ c,
+                                     const int *__restrict__ m, const int *__restrict__ n,
+                                     const int *__restrict__ o, double *coef, int *exps, int *off,
+                                     int *status)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0)
+        return;
+    int nt = 0;
+    for (int A = 0; A < nN; A++) {
+        off[A] = nt;
+        for (int p = 0; p < nB; p++) {
+            const int k = p + nB * A;
+            const int mm = m[k], nn = n[k], oo = o[k];
+            if (mm < 0 || mm > kMaxExp || nn < 0 || nn > kMaxExp || oo < 0 || oo > kMaxExp) {
+                *status = CUTC_ERR_INVALID;
+                continue;
+            }
+            const double cc = c[k];
+            if (!(fabs(cc) >= 1e-10))
+                continue;
+            if (nt >= kMaxTerms) {
+                *status = CUTC_ERR_INVALID;
+                continue;
+            }
+            coef[3 * nt] = cc * mm;
+            coef[3 * nt + 1] = cc * nn;
+            coef[3 * nt + 2] = cc * oo;
+            exps[nt] = mm | (nn << 3) | (oo << 6);
+            nt++;
+        }
+    }
+    off[nN] = nt;
+}
+
+// Device address of the scratch, looked up once per device with that device
+// current (the host-side name of a __device__ array is only a stand-in).
+static int noalloc_scratch(unsigned char **out)
+{
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static unsigned char *addr[kMaxDevices] = {};
+    int dev = 0;
+    CUTC_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        cutc_set_error(CUTC_ERR_NO_DEVICE, "device ordinal %d out of range", dev);
+        return CUTC_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            cutc_set_error(CUTC_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+            return CUTC_ERR_CUDA;
+        }
+        addr[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = addr[dev];
+    return CUTC_OK;
+}
+
+}  // namespace cutc
+
+extern "C" int cutc_jast_bh_dev_noalloc(int i0, int n1b, int n_grid1, int n_grid2, int n_nuc,
+                                        int size_bh, const double *r1, const double *r2,
+                                        const double *rn, const double *c_bh, const int *m_bh,
+                                        const int *n_bh, const int *o_bh, double a_en, double a_ee,
+                                        double *grad1u, void *stream)
+{
+    using namespace cutc;
+    if (n1b <= 0 || n_grid2 <= 0 || n_nuc <= 0 || size_bh < 0 || i0 < 0 || i0 + n1b > n_grid1 ||
+        n_nuc > kMaxNuc || !r1 || !r2 || !rn || !grad1u || !(a_en > 0) || !(a_ee > 0) ||
+        (size_bh > 0 && (!c_bh || !m_bh || !n_bh || !o_bh))) {
+        cutc_set_error(CUTC_ERR_INVALID, "invalid pair-kernel arguments");
+        return CUTC_ERR_INVALID;
+    }
+    const size_t need = kNaT1 + (size_t)n1b * n_nuc * sizeof(NucTerm) +
+                        (size_t)n_nuc * n_grid2 * sizeof(double) + 256;
+    if (need > kNoAllocScratchBytes) {
+        cutc_set_error(CUTC_ERR_INVALID,
+                       "%zu bytes of scratch needed (n1b=%d, n_grid2=%d, n_nuc=%d) exceed the "
+                       "%zu-byte static scratch of the allocation-free entry point",
+                       need, n1b, n_grid2, n_nuc, kNoAllocScratchBytes);
+        return CUTC_ERR_INVALID;
+    }
+    unsigned char *base = nullptr;
+    CUTC_TRY(noalloc_scratch(&base));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int *status = reinterpret_cast<int *>(base + kNaStatus);
+    double *coef = reinterpret_cast<double *>(base + kNaCoef);
+    int *exps = reinterpret_cast<int *>(base + kNaExps);
+    int *off = reinterpret_cast<int *>(base + kNaOff);
+    NucTerm *t1 = reinterpret_cast<NucTerm *>(base + kNaT1);
+    const size_t t1_bytes = ((size_t)n1b * n_nuc * sizeof(NucTerm) + 255) & ~(size_t)255;
+    double *f2 = reinterpret_cast<double *>(base + kNaT1 + t1_bytes);
+
+    // the scratch keeps the previous call's contents: only the status must start at zero
+    CUTC_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
+    noalloc_terms_kernel<<<1, 1, 0, st>>>(n_nuc, size_bh, c_bh, m_bh, n_bh, o_bh, coef, exps, off,
+                                          status);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    CUTC_TRY(launch_r1_terms(st, i0, n1b, n_nuc, r1, rn, a_en, t1));
+    CUTC_TRY(launch_r2_terms(st, n_grid2, n_nuc, r2, rn, a_en, f2));
+    PairArgs P;
+    P.i0 = i0; P.n1b = n1b; P.n2 = n_grid2; P.nN = n_nuc;
+    // the kernel reads the term count from off[nN]; size its shared memory for the maximum
+    P.n_terms = std::min(kMaxTerms, n_nuc * size_bh);
+    P.r1 = r1; P.r2 = r2; P.t1 = t1; P.f2 = f2;
+    P.coef = coef; P.exps = exps; P.term_off = off; P.a_ee = a_ee;
+    P.G = grad1u; P.ldg = n_grid2; P.plane = (int64_t)n1b * n_grid2;
+    CUTC_TRY(launch_pair_f64(st, P));
+    note_launches(4);
+    int h_status = 0;
+    CUTC_CUDA_TRY(cudaMemcpyAsync(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUTC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (h_status != CUTC_OK) {
+        cutc_set_error(h_status, "Jastrow exponent outside [0, %d] or more than %d terms", kMaxExp,
+                       kMaxTerms);
+        return h_status;
+    }
+    return CUTC_OK;
+}

@@ -111,6 +111,32 @@ int cutc_jast_bh_dev(int i0, int n1b, int n_grid1, int n_grid2, int n_nuc, int s
                      double a_en, double a_ee, double *grad1u);
 
 /*
+ * cutc_jast_bh_dev without any allocation, for callers that cannot let a
+ * library allocate device memory: code being captured into a CUDA graph or
+ * running in a latency-critical serving loop (cudaMalloc and cudaFree
+ * synchronise the device and are not allowed during capture), and programs
+ * whose own memory manager owns the whole device.  No counterpart in the
+ * reference.
+ *
+ * Same arguments, layout and results as cutc_jast_bh_dev, plus the stream to
+ * run on (NULL = the legacy default stream); synchronous on that stream.  Its
+ * scratch -- per-point nucleus terms, r2 e-n terms and the Jastrow term table,
+ * 32 * n1b * n_nuc + 8 * n_grid2 * n_nuc bytes plus ~130 KB -- lives in a
+ * fixed 32 MiB device array that every GPU loading this library holds until
+ * exit; larger requests are rejected with CUTC_ERR_INVALID and a message.  It
+ * calls no cudaMalloc, cudaFree or allocating library routine and creates no
+ * engine context.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress, with that device current): make that first
+ * call before any stream capture.  All calls share the one array, so calls
+ * that overlap on the GPU (different streams or threads) race: serialise them.
+ */
+int cutc_jast_bh_dev_noalloc(int i0, int n1b, int n_grid1, int n_grid2, int n_nuc, int size_bh,
+                             const double *r1, const double *r2, const double *rn,
+                             const double *c_bh, const int *m_bh, const int *n_bh,
+                             const int *o_bh, double a_en, double a_ee, double *grad1u,
+                             void *stream);
+
+/*
  * The split-precision contraction alone, on device arrays of the current
  * device: C[m + ldc * n] = sum_k A[m * K + k] * B[n * K + k] for m < M, n < N,
  * with A and B FP64 row-major (K contiguous) and the product formed from
