@@ -225,7 +225,8 @@ def run_ours(args):
     Xd = torch.empty((3, p.n_grid1, nA2), dtype=torch.float64, device=dev)
     Id = torch.empty((nA2, nA2), dtype=torch.float64, device=dev)
     stream = torch.cuda.Stream(device=dev)
-    opt = cg.options(prec, args.slices, p.a_en, p.a_ee, 3, True, 0, stream.cuda_stream)
+    opt = cg.options(prec, args.slices, p.a_en, p.a_ee, 3, True, 0, stream.cuda_stream,
+                     k_split=args.k_split)
 
     def build_device(stats=None):
         s = cg.cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
@@ -285,7 +286,8 @@ def run_ours(args):
     hp = {k: pinned(v) for k, v in p.arrays().items()}
     Xh = torch.empty((3, p.n_grid1, nA2), dtype=torch.float64, pin_memory=True).numpy()
     Ih = torch.empty((nA2, nA2), dtype=torch.float64, pin_memory=True).numpy()
-    opt_h = cg.options(prec, args.slices, p.a_en, p.a_ee, 3, False, 0, stream.cuda_stream)
+    opt_h = cg.options(prec, args.slices, p.a_en, p.a_ee, 3, False, 0, stream.cuda_stream,
+                       k_split=args.k_split)
 
     def build_host():
         s = cg.cutc_int_ex(opt_h, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
@@ -338,6 +340,7 @@ def run_ours(args):
                "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
                "config": {"workload": workload_desc(args.config, p),
                           "precision": args.precision, "n_slices": S if prec else None,
+                          "k_split": args.k_split,
                           "l2": "inputs larger than L2: per-build working set of tens of GB",
                           "parallelism": "replicas" if world > 1 else "1 GPU"},
                "gpu_launches": launches,
@@ -379,6 +382,72 @@ def run_ours(args):
     return 0
 
 
+def serving_requests(n, max_ao, seed=4004):
+    """The serving stream: molecules of 2-20 nuclei, n_ao uniform in [10, max_ao],
+    n_grid1 = 1000 n_nuc, n_grid2 = 4000 n_nuc; 30% repeat an earlier molecule with
+    Jastrow coefficients perturbed by a 10% Gaussian."""
+    import dataclasses
+    rng = np.random.default_rng(seed)
+    mols, reqs = [], []
+    for i in range(n):
+        if mols and rng.random() < 0.3:
+            k = int(rng.integers(len(mols)))
+            p = mols[k]
+            p = dataclasses.replace(p, c_bh=np.ascontiguousarray(
+                p.c_bh * (1.0 + 0.1 * rng.standard_normal(p.c_bh.shape))))
+            reqs.append((k + 1, p))
+        else:
+            nn = int(rng.integers(2, 21))
+            na = int(rng.integers(10, max_ao + 1))
+            p = synth.make_problem(n_nuc=nn, n_ao=na, n_grid1=1000 * nn, n_grid2=4000 * nn,
+                                   size_bh=9, seed=int(rng.integers(1 << 30)), box=1.5 + 0.4 * nn)
+            mols.append(p)
+            reqs.append((len(mols), p))
+    return reqs
+
+
+def run_serving(args):
+    """Poisson arrivals into the continuous-batching server; p50/p99 latency and builds/s."""
+    import cutc_gb300 as cg
+    import torch
+    torch.cuda.set_device(0)
+    reqs = serving_requests(args.requests, args.max_ao)
+    log("serving: %d requests generated" % len(reqs))
+    prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
+    rng = np.random.default_rng(7)
+    gaps = rng.exponential(1.0 / args.rate, size=len(reqs))
+    lat = []
+    with cg.Server(n_slots=args.slots) as srv:
+        t0 = time.perf_counter()
+        tickets = []
+        t_next = t0
+        for (key, p), gap in zip(reqs, gaps):
+            t_next += gap
+            while time.perf_counter() < t_next:
+                time.sleep(min(0.001, max(0.0, t_next - time.perf_counter())))
+            tickets.append(srv.submit(p, key, prec, args.slices))
+            # bound host memory: collect finished requests in order
+            while len(tickets) > 4 * args.slots:
+                lat.append(srv.wait(tickets.pop(0))[2])
+        for t in tickets:
+            lat.append(srv.wait(t)[2])
+        elapsed = time.perf_counter() - t0
+        st = srv.stats()
+    flops = sum(p.flops() for _, p in reqs)
+    line = {"metric": "TC integral builds/s and latency, serving stream", "value": len(reqs) / elapsed,
+            "unit": "builds/s", "n_gpus": 1, "higher_is_better": True,
+            "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
+            "config": {"workload": "serving: %d requests, Poisson arrivals at %.1f/s, 2-20 nuclei, "
+                                   "n_ao in [10, %d], n_grid1 = 1000 n_nuc, n_grid2 = 4000 n_nuc, "
+                                   "30%% repeats with perturbed Jastrow coefficients"
+                                   % (len(reqs), args.rate, args.max_ao),
+                       "slots": args.slots, "precision": args.precision},
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "server": st, "alg_tflops": flops / elapsed / 1e12}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def traffic_per_launch(args, p, launches):
     """DRAM bytes per X-contraction launch from the committed ncu summary, or None."""
     path = os.path.join(ROOT, "profiles", "split_gemm_traffic.json")
@@ -405,9 +474,18 @@ def main(argv=None):
     ap.add_argument("--config", default="medium", choices=sorted(synth.CONFIGS))
     ap.add_argument("--precision", choices=["split", "plain"], default="split")
     ap.add_argument("--slices", type=int, default=5)
+    ap.add_argument("--k-split", type=int, default=0,
+                    help="max K per tensor-core launch (0 = library default)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--serving", action="store_true", help="run the serving stream instead")
+    ap.add_argument("--requests", type=int, default=256)
+    ap.add_argument("--rate", type=float, default=8.0, help="serving arrivals per second")
+    ap.add_argument("--max-ao", type=int, default=120)
+    ap.add_argument("--slots", type=int, default=4)
     args = ap.parse_args(argv)
+    if args.serving:
+        return run_serving(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

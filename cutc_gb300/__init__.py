@@ -31,7 +31,8 @@ SPLIT_BF16 = 1
 # every symbol include/cutc_int.h declares
 EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_default_options", "cutc_jast_bh_dev",
            "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_validate_launch_dims",
-           "cutc_last_error", "cutc_release"]
+           "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
+           "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy"]
 
 
 class Options(ctypes.Structure):
@@ -48,6 +49,32 @@ class Stats(ctypes.Structure):
                 ("ms_int2e", ctypes.c_double), ("ms_d2h", ctypes.c_double),
                 ("n_r1_tiles", ctypes.c_int), ("gpu_launches", ctypes.c_int),
                 ("ms_x_gemm", ctypes.c_double), ("n_x_gemm", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("n_slots", ctypes.c_int), ("device_budget_bytes", ctypes.c_size_t),
+                ("cache_budget_bytes", ctypes.c_size_t), ("tile_budget_bytes", ctypes.c_size_t)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("molecule_key", ctypes.c_ulonglong)] + \
+        [(k, ctypes.c_int) for k in ("n_grid1", "n_grid2", "n_ao", "n_nuc", "size_bh")] + \
+        [(k, ctypes.c_void_p) for k in ("r1", "wr1", "r2", "wr2", "rn", "aos_data1", "aos_data2",
+                                        "c_bh", "m_bh", "n_bh", "o_bh", "int2_grad1_u12_ao",
+                                        "int_2e_ao")] + \
+        [("options", Options)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_long), ("failed", ctypes.c_long), ("queued", ctypes.c_long),
+                ("in_flight", ctypes.c_int), ("peak_in_flight", ctypes.c_int),
+                ("cache_hits", ctypes.c_long), ("cache_misses", ctypes.c_long),
+                ("cache_bytes", ctypes.c_size_t), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+                ("builds_per_s", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -90,6 +117,18 @@ def load(path: str = LIB_PATH):
     L.cutc_last_error.restype = ctypes.c_char_p
     L.cutc_release.argtypes = []
     L.cutc_release.restype = None
+    L.cutc_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
+    L.cutc_server_default_config.restype = None
+    L.cutc_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
+    L.cutc_server_create.restype = i
+    L.cutc_server_submit.argtypes = [vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_ulonglong)]
+    L.cutc_server_submit.restype = i
+    L.cutc_server_wait.argtypes = [vp, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_double)]
+    L.cutc_server_wait.restype = i
+    L.cutc_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+    L.cutc_server_get_stats.restype = i
+    L.cutc_server_destroy.argtypes = [vp]
+    L.cutc_server_destroy.restype = None
     _lib = L
     return L
 
@@ -202,3 +241,73 @@ def split_gemm_device(A, B, C=None, n_slices=5):
     if s != CUTC_OK:
         raise CutcError(s, last_error())
     return C.T
+
+
+class Server:
+    """Continuous-batching integral-build server on the current GPU (C-ABI cutc_server_*).
+
+    submit() takes a synth.Problem (host arrays), returns a ticket immediately and
+    keeps the arrays alive until wait(ticket) returns (X, int_2e, latency_ms).
+    """
+
+    def __init__(self, n_slots=4, device_budget_bytes=0, cache_budget_bytes=0,
+                 tile_budget_bytes=0):
+        L = load()
+        cfg = ServerConfig()
+        L.cutc_server_default_config(ctypes.byref(cfg))
+        cfg.n_slots = n_slots
+        cfg.device_budget_bytes = device_budget_bytes
+        cfg.cache_budget_bytes = cache_budget_bytes
+        if tile_budget_bytes:
+            cfg.tile_budget_bytes = tile_budget_bytes
+        self._h = ctypes.c_void_p()
+        s = L.cutc_server_create(ctypes.byref(cfg), ctypes.byref(self._h))
+        if s != CUTC_OK:
+            raise CutcError(s, last_error())
+        self._live = {}
+
+    def submit(self, p, molecule_key=0, precision=PLAIN_FP64, n_slices=None, x_components=3):
+        X = np.empty((x_components, p.n_grid1, p.n_ao ** 2))
+        I = np.empty((p.n_ao ** 2, p.n_ao ** 2))
+        arrs = p.arrays()
+        q = Request()
+        q.molecule_key = molecule_key
+        q.n_grid1, q.n_grid2, q.n_ao, q.n_nuc, q.size_bh = (p.n_grid1, p.n_grid2, p.n_ao,
+                                                           p.n_nuc, p.size_bh)
+        for k, name in (("r1", "r1"), ("wr1", "wr1"), ("r2", "r2"), ("wr2", "wr2"), ("rn", "rn"),
+                        ("aos1", "aos_data1"), ("aos2", "aos_data2"), ("c_bh", "c_bh"),
+                        ("m_bh", "m_bh"), ("n_bh", "n_bh"), ("o_bh", "o_bh")):
+            setattr(q, name, arrs[k].ctypes.data)
+        q.int2_grad1_u12_ao = X.ctypes.data
+        q.int_2e_ao = I.ctypes.data
+        q.options = options(precision, n_slices, p.a_en, p.a_ee, x_components)
+        t = ctypes.c_ulonglong()
+        s = load().cutc_server_submit(self._h, ctypes.byref(q), ctypes.byref(t))
+        if s != CUTC_OK:
+            raise CutcError(s, last_error())
+        self._live[t.value] = (p, X, I, q)
+        return t.value
+
+    def wait(self, ticket):
+        lat = ctypes.c_double()
+        s = load().cutc_server_wait(self._h, ticket, ctypes.byref(lat))
+        p, X, I, q = self._live.pop(ticket)
+        if s != CUTC_OK:
+            raise CutcError(s, last_error())
+        return X, I, lat.value
+
+    def stats(self):
+        st = ServerStats()
+        load().cutc_server_get_stats(self._h, ctypes.byref(st))
+        return st.as_dict()
+
+    def close(self):
+        if self._h:
+            load().cutc_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -104,6 +104,56 @@ void Workspace::release()
 static std::mutex g_engines_mu;
 static std::vector<Engine *> g_engines;
 
+int make_engine(int dev, Engine **out)
+{
+    cudaDeviceProp prop;
+    CUTC_CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
+    if (prop.major != 10 || prop.minor != 3) {
+        cutc_set_error(CUTC_ERR_NO_DEVICE,
+                       "device %d is sm_%d%d; this library is built for sm_103a (GB300)", dev,
+                       prop.major, prop.minor);
+        return CUTC_ERR_NO_DEVICE;
+    }
+    Engine *E = new Engine();
+    E->device = dev;
+    E->n_sm = prop.multiProcessorCount;
+    E->max_threads_per_block = prop.maxThreadsPerBlock;
+    for (int k = 0; k < 3; k++)
+        E->max_grid[k] = prop.maxGridSize[k];
+    cudaError_t e = cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        for (int k = 0; k < kNumEvents && e == cudaSuccess; k++)
+            e = cudaEventCreate(&E->ev[k]);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cutc_set_error(CUTC_ERR_CUDA, "engine setup: %s", cudaGetErrorString(e));
+        delete E;
+        return CUTC_ERR_CUDA;
+    }
+    if (cublasCreate(&E->blas) != CUBLAS_STATUS_SUCCESS) {
+        cutc_set_error(CUTC_ERR_CUDA, "cublasCreate failed");
+        delete E;
+        return CUTC_ERR_CUDA;
+    }
+    *out = E;
+    return CUTC_OK;
+}
+
+void destroy_engine(Engine *E)
+{
+    if (!E)
+        return;
+    cudaStreamSynchronize(E->stream);
+    E->ws.release();
+    for (auto e : E->tile_ev)
+        cudaEventDestroy(e);
+    for (int k = 0; k < kNumEvents; k++)
+        cudaEventDestroy(E->ev[k]);
+    cublasDestroy(E->blas);
+    cudaStreamDestroy(E->stream);
+    delete E;
+}
+
 int get_engine(Engine **out)
 {
     int dev = 0;
@@ -116,30 +166,8 @@ int get_engine(Engine **out)
     std::lock_guard<std::mutex> lk(g_engines_mu);
     if ((int)g_engines.size() <= dev)
         g_engines.resize(dev + 1, nullptr);
-    if (!g_engines[dev]) {
-        cudaDeviceProp prop;
-        CUTC_CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
-        if (prop.major != 10 || prop.minor != 3) {
-            cutc_set_error(CUTC_ERR_NO_DEVICE,
-                           "device %d is sm_%d%d; this library is built for sm_103a (GB300)", dev,
-                           prop.major, prop.minor);
-            return CUTC_ERR_NO_DEVICE;
-        }
-        Engine *E = new Engine();
-        E->device = dev;
-        E->n_sm = prop.multiProcessorCount;
-        E->max_threads_per_block = prop.maxThreadsPerBlock;
-        for (int k = 0; k < 3; k++)
-            E->max_grid[k] = prop.maxGridSize[k];
-        CUTC_CUDA_TRY(cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking));
-        if (cublasCreate(&E->blas) != CUBLAS_STATUS_SUCCESS) {
-            cutc_set_error(CUTC_ERR_CUDA, "cublasCreate failed");
-            return CUTC_ERR_CUDA;
-        }
-        for (int k = 0; k < kNumEvents; k++)
-            CUTC_CUDA_TRY(cudaEventCreate(&E->ev[k]));
-        g_engines[dev] = E;
-    }
+    if (!g_engines[dev])
+        CUTC_TRY(make_engine(dev, &g_engines[dev]));
     *out = g_engines[dev];
     return CUTC_OK;
 }
@@ -258,6 +286,31 @@ static size_t r1_row_bytes(const Request &R)
     return g;
 }
 
+size_t build_footprint(const Request &R, size_t tile_budget)
+{
+    const int64_t n1 = R.n1, n2 = R.n2, nA = R.nA, nN = R.nN;
+    const int64_t np = n_pairs(nA), nl = std::max<int64_t>(1, n_strict_pairs(nA)), nA2 = nA * nA;
+    const int64_t n1t = std::max<int64_t>(1, std::min<int64_t>(n1, (int64_t)(tile_budget / r1_row_bytes(R))));
+    auto up = [](int64_t a, int64_t b) { return (a + b - 1) / b * b; };
+    double b = 0;
+    b += 4.0 * n1t * n2 * 8 + (double)n1t * nN * sizeof(NucTerm) + (double)nN * n2 * 8;
+    b += 4.0 * n1 * np * 8;
+    if (!(R.device_pointers || R.out_device))
+        b += ((double)R.x_components * n1 * nA2 + (double)nA2 * nA2) * 8;
+    if (!(R.device_pointers || R.in_device))
+        b += (4.0 * n1 + 4.0 * n2 + 3.0 * nN + 4.0 * n1 * nA + (double)n2 * nA) * 8;
+    if (R.precision == CUTC_PLAIN_FP64) {
+        b += ((double)np * n2 + (double)np * n1 + 3.0 * nl * n1 + (double)np * np + (double)np * nl) * 8;
+    } else {
+        const double S2 = 2.0 * R.n_slices;
+        b += S2 * up(np, 128) * up(n2, 32) + S2 * up(4 * n1t, 48) * up(n2, 32);
+        b += S2 * (up(np, 128) * up(n1, 32) + up(np, 128) * up(3 * n1, 32) + up(np, 48) * up(n1, 32) +
+                   up(nl, 48) * up(3 * n1, 32));
+        b += ((double)np * np + (double)np * nl) * 8 + (4.0 * n2 + nN * n2) * 8 + n1t * nN * 91.0 * 8;
+    }
+    return (size_t)(b * 1.05) + ((size_t)64 << 20);
+}
+
 int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
 {
     CUTC_TRY(validate(R_in));
@@ -266,7 +319,7 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     // parameters are brought over first (they are tiny: size_bh x n_nuc).
     std::vector<double> h_c;
     std::vector<int> h_m, h_n, h_o;
-    if (R.device_pointers && R.nB > 0) {
+    if (R.device_pointers && R.nB > 0) {  // Jastrow parameters on the device
         const size_t nt_in = (size_t)R.nB * R.nN;
         cudaStream_t s0 = R.stream ? R.stream : E->stream;
         h_c.resize(nt_in);
@@ -305,12 +358,12 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         *dst = (const double *)p;
         return CUTC_OK;
     };
-    if (R.device_pointers) {
+    const bool in_dev = R.device_pointers || R.in_device;
+    const bool out_dev = R.device_pointers || R.out_device;
+    if (in_dev) {
         d_r1 = R.r1; d_wr1 = R.wr1; d_r2 = R.r2; d_wr2 = R.wr2; d_rn = R.rn;
         d_aos1 = R.aos1;
         d_aos2v = R.aos2;  // component 0 is the first n2*nA block
-        d_X = R.X;
-        d_I = R.I;
     } else {
         CUTC_TRY(put(S_R1, R.r1, 3 * (size_t)n1 * 8, &d_r1));
         CUTC_TRY(put(S_WR1, R.wr1, (size_t)n1 * 8, &d_wr1));
@@ -320,6 +373,11 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         CUTC_TRY(put(S_AOS1, R.aos1, 4 * (size_t)n1 * nA * 8, &d_aos1));
         // only the value component of aos_data2 is used (src/long_range_integ.cu:30-35)
         CUTC_TRY(put(S_AOS2, R.aos2, (size_t)n2 * nA * 8, &d_aos2v));
+    }
+    if (out_dev) {
+        d_X = R.X;
+        d_I = R.I;
+    } else {
         CUTC_TRY(W.get(S_XOUT, (size_t)R.x_components * n1 * nA2 * 8, &p));
         d_X = (double *)p;
         CUTC_TRY(W.get(S_IOUT, (size_t)nA2 * nA2 * 8, &p));
@@ -489,7 +547,7 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     CUTC_TRY(launch_expand_pairs(st, (int64_t)R.x_components * n1, nA, d_Xp, np, d_X));
     note_launches(1);
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[7], st));
-    if (!R.device_pointers) {
+    if (!out_dev) {
         CUTC_CUDA_TRY(cudaMemcpyAsync(R.X, d_X, (size_t)R.x_components * n1 * nA2 * 8,
                                       cudaMemcpyDeviceToHost, st));
         CUTC_CUDA_TRY(cudaMemcpyAsync(R.I, d_I, (size_t)nA2 * nA2 * 8, cudaMemcpyDeviceToHost, st));

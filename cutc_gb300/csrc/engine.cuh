@@ -43,7 +43,9 @@ struct Request {
     int n_slices = 5;
     double a_en = 1.0, a_ee = 1.0;
     int x_components = 3;
-    int device_pointers = 0;
+    int device_pointers = 0;  // every array on the device
+    int in_device = 0;        // molecule arrays (r1 .. aos2) on the device
+    int out_device = 0;       // X and int_2e on the device
     size_t max_work_bytes = 0;
     int tile_rows = 0;  // optional cap on r1 rows per tile
     int pair_fp64 = 0;  // split form: FP64 pair terms
@@ -58,6 +60,11 @@ struct Request {
 };
 
 int get_engine(Engine **out);
+// A private execution context (stream, cuBLAS handle, events, workspace) on device dev.
+int make_engine(int dev, Engine **out);
+void destroy_engine(Engine *E);
+// Device bytes one build needs besides its molecule arrays, for a given r1-tile budget.
+size_t build_footprint(const Request &R, size_t tile_budget);
 int build_terms(const Request &R, std::vector<double> &coef, std::vector<int> &exps,
                 std::vector<int> &off);
 int run_build(Engine *E, const Request &R, cutc_stats *stats);

@@ -156,6 +156,54 @@ int cutc_split_gemm_dev(int n_slices, int M, int N, long long K,
 int cutc_validate_launch_dims(int nxBlocks, int nyBlocks, int nzBlocks,
                               int blockxSize, int blockySize, int blockzSize);
 
+/* ---- serving: continuous batching on one GPU (no reference counterpart) --
+ * A server owns n_slots execution contexts (stream, cuBLAS handle,
+ * workspace) and a worker thread each.  Submitted requests are queued; a free
+ * worker takes the first queued request whose device footprint fits the
+ * memory budget next to the requests in flight (a request that does not fit
+ * runs alone), so requests overlap on the GPU as slots and memory free up.
+ * Requests with a non-zero molecule_key keep their molecule arrays (grids,
+ * weights, nuclei, AO values) resident in a byte-budgeted LRU cache: a later
+ * request with the same key and sizes copies only its Jastrow parameters.
+ * All array pointers of a request are host pointers and must stay valid until
+ * cutc_server_wait returns for it.  Each result is the same as the one a
+ * standalone cutc_int_ex call with the same options gives. */
+typedef struct cutc_server cutc_server;
+
+typedef struct cutc_server_config {
+    int n_slots;                /* concurrent requests on the GPU (default 4) */
+    size_t device_budget_bytes; /* admission budget for requests in flight (0: 3/4 of free) */
+    size_t cache_budget_bytes;  /* molecule cache (0: 1/4 of the device budget) */
+    size_t tile_budget_bytes;   /* r1-tile working set per request (default 4 GiB) */
+} cutc_server_config;
+
+typedef struct cutc_request {
+    unsigned long long molecule_key; /* 0: no caching; else identifies the molecule arrays */
+    int n_grid1, n_grid2, n_ao, n_nuc, size_bh;
+    const double *r1, *wr1, *r2, *wr2, *rn, *aos_data1, *aos_data2, *c_bh;
+    const int *m_bh, *n_bh, *o_bh;
+    double *int2_grad1_u12_ao, *int_2e_ao;
+    cutc_options options;       /* device_pointers, stream and max_work_bytes are ignored */
+} cutc_request;
+
+typedef struct cutc_server_stats {
+    long completed, failed, queued;
+    int in_flight, peak_in_flight;
+    long cache_hits, cache_misses;
+    size_t cache_bytes;
+    double p50_ms, p99_ms, max_ms;  /* submit-to-completion latency of completed requests */
+    double builds_per_s;            /* completed / (last completion - first submit) */
+} cutc_server_stats;
+
+void cutc_server_default_config(cutc_server_config *cfg);
+int cutc_server_create(const cutc_server_config *cfg, cutc_server **server);
+int cutc_server_submit(cutc_server *server, const cutc_request *req, unsigned long long *ticket);
+/* Blocks until the request is done; returns its status and forgets the ticket. */
+int cutc_server_wait(cutc_server *server, unsigned long long ticket, double *latency_ms);
+int cutc_server_get_stats(cutc_server *server, cutc_server_stats *stats);
+/* Finishes the queued requests, then frees the contexts and the cache. */
+void cutc_server_destroy(cutc_server *server);
+
 /* Message describing the last non-zero status returned on this thread. */
 const char *cutc_last_error(void);
 
