@@ -448,6 +448,62 @@ def run_serving(args):
     return 0
 
 
+def run_scan(args):
+    """Batched Jastrow-parameter scan: one molecule, n_sets parameter sets."""
+    import dataclasses
+    import cutc_gb300 as cg
+    import torch
+    from oracle.oracle import rel_err
+    torch.cuda.set_device(0)
+    p = synth.make_config("scan")
+    rng = np.random.default_rng(5050)
+    ns = args.sets
+    c_sets = rng.normal(0.0, 0.3, size=(ns,) + p.c_bh.shape)
+    a_en = rng.uniform(0.5, 2.0, ns)
+    a_ee = rng.uniform(0.5, 2.0, ns)
+    prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
+    batch = min(ns, args.scan_batch)
+    log("scan: warm-up")
+    cg.scan_integrals(p, c_sets[:1], a_en[:1], a_ee[:1], prec, args.slices)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    launches = 0
+    for b0 in range(0, ns, batch):
+        sl = slice(b0, min(ns, b0 + batch))
+        X, I, st = cg.scan_integrals(p, c_sets[sl], a_en[sl], a_ee[sl], prec, args.slices,
+                                     with_stats=True)
+        launches += st["gpu_launches"]
+        del X, I
+    elapsed = time.perf_counter() - t0
+    log("scan: %.3f sets/s; accuracy sample" % (ns / elapsed))
+    rows = 256
+    i0 = (p.n_grid1 // 2) // 64 * 64
+    sub = dataclasses.replace(p, r1=np.ascontiguousarray(p.r1[i0:i0 + rows]),
+                              wr1=np.ascontiguousarray(p.wr1[i0:i0 + rows]),
+                              aos1=np.ascontiguousarray(p.aos1[:, :, i0:i0 + rows]))
+    Xs, Is = cg.scan_integrals(sub, c_sets, a_en, a_ee, prec, args.slices)
+    Xp, Ip = cg.scan_integrals(sub, c_sets, a_en, a_ee, cg.PLAIN_FP64)
+    ex = [rel_err(Xs[k], Xp[k]) for k in range(ns)]
+    ei = [rel_err(Is[k], Ip[k]) for k in range(ns)]
+    line = {"metric": "TC integral builds/s, Jastrow-parameter scan", "value": ns / elapsed,
+            "unit": "builds/s", "n_gpus": 1, "higher_is_better": True,
+            "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
+            "config": {"workload": "scan: " + workload_desc("scan", p) + ", %d Jastrow parameter "
+                                   "sets (c ~ N(0, 0.3), a_en, a_ee ~ U[0.5, 2]), %d sets per "
+                                   "cutc_int_scan call" % (ns, batch),
+                       "precision": args.precision},
+            "gpu_launches": launches,
+            "alg_tflops": ns * p.flops() / elapsed / 1e12,
+            "accuracy": {"X_vs_fp64_max_over_sets": max(e["norm"] for e in ex),
+                         "X_vs_fp64_maxabs_max_over_sets": max(e["max"] for e in ex),
+                         "int2e_vs_fp64_max_over_sets": max(e["norm"] for e in ei),
+                         "int2e_vs_fp64_maxabs_max_over_sets": max(e["max"] for e in ei),
+                         "sample": "%d of %d r1 rows, every set; split vs the plain FP64 form"
+                                   % (rows, p.n_grid1)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def traffic_per_launch(args, p, launches):
     """DRAM bytes per X-contraction launch from the committed ncu summary, or None."""
     path = os.path.join(ROOT, "profiles", "split_gemm_traffic.json")
@@ -483,9 +539,14 @@ def main(argv=None):
     ap.add_argument("--rate", type=float, default=8.0, help="serving arrivals per second")
     ap.add_argument("--max-ao", type=int, default=120)
     ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--scan", action="store_true", help="run the Jastrow-parameter scan instead")
+    ap.add_argument("--sets", type=int, default=64)
+    ap.add_argument("--scan-batch", type=int, default=8)
     args = ap.parse_args(argv)
     if args.serving:
         return run_serving(args)
+    if args.scan:
+        return run_scan(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -29,7 +29,7 @@ PLAIN_FP64 = 0
 SPLIT_BF16 = 1
 
 # every symbol include/cutc_int.h declares
-EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_default_options", "cutc_jast_bh_dev",
+EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_int_scan", "cutc_default_options", "cutc_jast_bh_dev",
            "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_validate_launch_dims",
            "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
            "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy"]
@@ -103,6 +103,9 @@ def load(path: str = LIB_PATH):
     L.cutc_int.restype = i
     L.cutc_int_ex.argtypes = [ctypes.POINTER(Options)] + [i] * 5 + [vp] * 13 + [ctypes.POINTER(Stats)]
     L.cutc_int_ex.restype = i
+    L.cutc_int_scan.argtypes = [ctypes.POINTER(Options), i] + [i] * 5 + [vp] * 15 + \
+        [ctypes.POINTER(Stats)]
+    L.cutc_int_scan.restype = i
     L.cutc_default_options.argtypes = [ctypes.POINTER(Options)]
     L.cutc_default_options.restype = None
     L.cutc_jast_bh_dev.argtypes = [i] * 6 + [vp] * 7 + [dp, dp, vp]
@@ -198,6 +201,35 @@ def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
     s = cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
                     p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2,
                     p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I, st)
+    if s != CUTC_OK:
+        raise CutcError(s, last_error())
+    return (X, I, st.as_dict()) if with_stats else (X, I)
+
+
+def scan_integrals(p, c_sets, a_en=None, a_ee=None, precision=PLAIN_FP64, n_slices=None,
+                   x_components=3, with_stats=False):
+    """Jastrow-parameter scan on one molecule (cutc_int_scan).
+
+    c_sets: (n_sets, n_nuc, size_bh) coefficients (the exponents of p are used for
+    every set); a_en / a_ee: per-set scale factors or None.  Returns
+    X (n_sets, x_components, n1, nA^2) and int_2e (n_sets, nA^2, nA^2).
+    """
+    c_sets = np.ascontiguousarray(c_sets, dtype=np.float64)
+    ns = c_sets.shape[0]
+    rep = lambda a: np.ascontiguousarray(np.broadcast_to(a, (ns,) + a.shape))
+    m, n, o = rep(p.m_bh), rep(p.n_bh), rep(p.o_bh)
+    ae = None if a_en is None else np.ascontiguousarray(a_en, dtype=np.float64)
+    aee = None if a_ee is None else np.ascontiguousarray(a_ee, dtype=np.float64)
+    X = np.empty((ns, x_components, p.n_grid1, p.n_ao ** 2))
+    I = np.empty((ns, p.n_ao ** 2, p.n_ao ** 2))
+    opt = options(precision, n_slices, p.a_en, p.a_ee, x_components)
+    st = Stats()
+    arrs = [p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2, c_sets, m, n, o]
+    s = load().cutc_int_scan(ctypes.byref(opt), ns, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc,
+                             p.size_bh, *[_vp(a) for a in arrs],
+                             _vp(ae) if ae is not None else None,
+                             _vp(aee) if aee is not None else None, _vp(X), _vp(I),
+                             ctypes.byref(st))
     if s != CUTC_OK:
         raise CutcError(s, last_error())
     return (X, I, st.as_dict()) if with_stats else (X, I)

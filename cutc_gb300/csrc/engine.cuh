@@ -34,6 +34,12 @@ struct Engine {
     cudaEvent_t ev[kNumEvents];
     std::vector<cudaEvent_t> tile_ev;  // per-tile timing events (grown on demand)
     Workspace ws;
+    // Molecule-dependent operands left in the workspace by the previous build:
+    // (molecule tag, buffer address) of the X-build A operand and of the int_2e
+    // B operands.  A build with the same non-zero tag and the same buffer skips
+    // rebuilding them.
+    uint64_t tag_x = 0, tag_i = 0;
+    const void *tag_x_buf = nullptr, *tag_i_buf = nullptr;
     std::mutex mu;
 };
 
@@ -50,6 +56,7 @@ struct Request {
     int tile_rows = 0;  // optional cap on r1 rows per tile
     int pair_fp64 = 0;  // split form: FP64 pair terms
     int k_split = 0;    // split form: max K per tensor-core launch (0 = default)
+    uint64_t mol_tag = 0;  // non-zero: molecule arrays identical to earlier builds with this tag
     cudaStream_t stream = nullptr;
     int n1 = 0, n2 = 0, nA = 0, nN = 0, nB = 0;
     const double *r1 = nullptr, *wr1 = nullptr, *r2 = nullptr, *wr2 = nullptr, *rn = nullptr;

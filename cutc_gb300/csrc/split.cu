@@ -748,7 +748,11 @@ int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *
     CUTC_TRY(alloc_operand(W, slot0 + SS_BX, R.n_slices, (int)(4 * n1t), bn_for(R.n_slices), R.n2,
                            S_.BX));
     SrcSym src{wr2, aos2v, (int64_t)R.n2, S_.pairs_sym};
+    if (R.mol_tag && E->tag_x == R.mol_tag && E->tag_x_buf == S_.AX.sl)
+        return CUTC_OK;  // the same molecule's P slices are already there
     CUTC_SLICES_DISPATCH(R.n_slices, CUTC_TRY((slice_rows<S, SrcSym>(st, src, S_.AX))));
+    E->tag_x = R.mol_tag;
+    E->tag_x_buf = S_.AX.sl;
     return CUTC_OK;
 }
 
@@ -795,16 +799,21 @@ int split_int2e(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, con
     double *N = (double *)p;
     SrcSym s0{wr1, aos1, (int64_t)n1, S_.pairs_sym};
     SrcAnti sa{wr1, aos1, n1, nA, S_.pairs_anti};
+    const bool reuse_b = R.mol_tag && E->tag_i == R.mol_tag && E->tag_i_buf == BH.sl;
     CUTC_SLICES_DISPATCH(sp.n_slices, {
         CUTC_TRY(slice_cols<S>(st, Xp, np, 3 * (int64_t)n1, AH));
         CUTC_TRY(slice_cols<S>(st, Xp, np, 0, AN));
-        CUTC_TRY((slice_rows<S, SrcSym>(st, s0, BH)));
+        if (!reuse_b)
+            CUTC_TRY((slice_rows<S, SrcSym>(st, s0, BH)));
         CUTC_TRY(gemm<S>(st, AH, BH, 1.0, H, np, np, 0, 0, 0, S_.err, R.k_split));
         if (nl > 0) {
-            CUTC_TRY((slice_rows<S, SrcAnti>(st, sa, BN)));
+            if (!reuse_b)
+                CUTC_TRY((slice_rows<S, SrcAnti>(st, sa, BN)));
             CUTC_TRY(gemm<S>(st, AN, BN, -0.5, N, np, nl, 0, 0, 0, S_.err, R.k_split));
         }
     });
+    E->tag_i = R.mol_tag;
+    E->tag_i_buf = BH.sl;
     CUTC_TRY(launch_assemble_int2e(st, nA, H, N, I));
     note_launches(1);
     int herr = 0;

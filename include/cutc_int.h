@@ -99,6 +99,26 @@ int cutc_int_ex(const cutc_options *opt,
                 double *int2_grad1_u12_ao, double *int_2e_ao, cutc_stats *stats);
 
 /*
+ * A Jastrow-parameter scan: the build of cutc_int_ex for n_sets parameter sets
+ * on one molecule.  The molecule arrays are copied to the device once and the
+ * Jastrow-independent operands (the AO pair products on both grids, or their
+ * BF16 slices) are built once and shared by all sets; only the pair terms and
+ * the contractions run per set.  Set s uses c/m/n/o_bh + s * size_bh * n_nuc,
+ * a_en[s] and a_ee[s] (NULL: opt->a_en / opt->a_ee) and writes its outputs at
+ * int2_grad1_u12_ao + s * x_components * n_grid1 * n_ao^2 and
+ * int_2e_ao + s * n_ao^4.  Each set's result equals the cutc_int_ex result
+ * with the same options.  stats (optional) sums the per-set statistics.
+ * No reference counterpart.
+ */
+int cutc_int_scan(const cutc_options *opt, int n_sets,
+                  int n_grid1, int n_grid2, int n_ao, int n_nuc, int size_bh,
+                  const double *r1, const double *wr1, const double *r2, const double *wr2,
+                  const double *rn, const double *aos_data1, const double *aos_data2,
+                  const double *c_bh, const int *m_bh, const int *n_bh, const int *o_bh,
+                  const double *a_en, const double *a_ee,
+                  double *int2_grad1_u12_ao, double *int_2e_ao, cutc_stats *stats);
+
+/*
  * Pair terms alone, on device pointers: for r1 rows [i0, i0 + n1b) and all
  * r2 points, writes grad1u[c * n1b * n2 + i * n2 + j] for c = 0..2 (gradient)
  * and c = 3 (-1/2 |grad1 u|^2): the layout of grad1_u12 in the reference's
