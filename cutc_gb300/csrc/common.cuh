@@ -9,20 +9,22 @@
 
 #define CUTC_CUDA_TRY(expr)                                                   \
     do {                                                                      \
-        cudaError_t e_ = (expr);                                              \
-        if (e_ != cudaSuccess) {                                              \
+        cudaError_t cutc_err_ = (expr);                                       \
+        if (cutc_err_ != cudaSuccess) {                                       \
             cutc_set_error(CUTC_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, \
-                           #expr, cudaGetErrorString(e_));                    \
-            return e_ == cudaErrorMemoryAllocation ? CUTC_ERR_NO_MEMORY       \
-                                                   : CUTC_ERR_CUDA;           \
+                           #expr, cudaGetErrorString(cutc_err_));             \
+            return cutc_err_ == cudaErrorMemoryAllocation ? CUTC_ERR_NO_MEMORY \
+                                                          : CUTC_ERR_CUDA;    \
         }                                                                     \
     } while (0)
 
-#define CUTC_TRY(expr)          \
-    do {                        \
-        int s_ = (expr);        \
-        if (s_ != CUTC_OK)      \
-            return s_;          \
+// (the status variable has a name no caller uses, so that expr may name any
+// variable of the caller)
+#define CUTC_TRY(expr)                    \
+    do {                                  \
+        int cutc_status_ = (expr);        \
+        if (cutc_status_ != CUTC_OK)      \
+            return cutc_status_;          \
     } while (0)
 
 // Records the message behind the last non-zero status (thread-local).

@@ -54,11 +54,11 @@ long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
 #define CUBLAS_TRY(expr)                                                              \
     do {                                                                              \
-        cublasStatus_t s_ = (expr);                                                   \
-        if (s_ != CUBLAS_STATUS_SUCCESS) {                                            \
+        cublasStatus_t cutc_blas_ = (expr);                                           \
+        if (cutc_blas_ != CUBLAS_STATUS_SUCCESS) {                                    \
             cutc_set_error(CUTC_ERR_CUDA, "%s:%d %s: cuBLAS status %d", __FILE__,     \
-                           __LINE__, #expr, (int)s_);                                 \
-            return s_ == CUBLAS_STATUS_ALLOC_FAILED ? CUTC_ERR_NO_MEMORY : CUTC_ERR_CUDA; \
+                           __LINE__, #expr, (int)cutc_blas_);                         \
+            return cutc_blas_ == CUBLAS_STATUS_ALLOC_FAILED ? CUTC_ERR_NO_MEMORY : CUTC_ERR_CUDA; \
         }                                                                             \
     } while (0)
 
@@ -122,6 +122,8 @@ int make_engine(int dev, Engine **out)
         E->max_grid[k] = prop.maxGridSize[k];
     cudaError_t e = cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&E->xfer, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
         for (int k = 0; k < kNumEvents && e == cudaSuccess; k++)
             e = cudaEventCreate(&E->ev[k]);
     if (e != cudaSuccess) {
@@ -150,6 +152,8 @@ void destroy_engine(Engine *E)
     for (int k = 0; k < kNumEvents; k++)
         cudaEventDestroy(E->ev[k]);
     cublasDestroy(E->blas);
+    cudaStreamSynchronize(E->xfer);
+    cudaStreamDestroy(E->xfer);
     cudaStreamDestroy(E->stream);
     delete E;
 }
@@ -265,7 +269,7 @@ static int validate(const Request &R)
 
 enum Slot {
     S_R1, S_WR1, S_R2, S_WR2, S_RN, S_AOS1, S_AOS2, S_COEF, S_EXPS, S_OFF,
-    S_T1, S_F2, S_P, S_G, S_XP, S_S0, S_SL, S_H, S_N, S_XOUT, S_IOUT,
+    S_T1, S_F2, S_P, S_G, S_XP, S_S0, S_SL, S_H, S_N, S_XOUT, S_XOUT1, S_IOUT, S_IOUT1,
     S_R2D, S_F2D, S_POLY,
     S_SPLIT0  // split-form slots follow
 };
@@ -277,39 +281,70 @@ static inline double ev_ms(cudaEvent_t a, cudaEvent_t b)
     return ms;
 }
 
-// Bytes per r1 row of the X-build working set (G tile, plus slices when split).
+// Columns of int_2e per output slab when int_2e goes to the host: a slab is
+// assembled on the device and copied out while the next one is assembled.
+// CUTC_INT2E_SLAB_COLS overrides the 1 GiB slab (rounded down to 32 columns).
+static int int2e_slab_cols(int nA)
+{
+    const int64_t n = (int64_t)nA * nA;
+    int64_t per = (((int64_t)1 << 30) / (n * 8)) / 32 * 32;
+    if (const char *e = getenv("CUTC_INT2E_SLAB_COLS"))
+        per = atoll(e) / 32 * 32;
+    return (int)std::min<int64_t>(n, std::max<int64_t>(32, per));
+}
+
+// Device bytes of a build that do not grow with the r1 tile (besides the
+// molecule arrays): r2 terms, the P operand, H and N, int_2e output slabs.
+static size_t fixed_bytes(const Request &R)
+{
+    const int64_t n2 = R.n2, nA = R.nA, nN = R.nN;
+    const int64_t np = n_pairs(nA), nl = std::max<int64_t>(1, n_strict_pairs(nA));
+    double b = (double)nN * n2 * 8 + ((double)np * np + (double)np * nl) * 8;
+    if (R.precision == CUTC_PLAIN_FP64)
+        b += (double)np * n2 * 8;
+    else
+        b += (double)split_fixed_bytes(R) + (3.0 + nN) * n2 * sizeof(float2);
+    if (!(R.device_pointers || R.out_device))
+        b += 2.0 * int2e_slab_cols(R.nA) * nA * nA * 8;
+    return (size_t)b;
+}
+
+// Device bytes per r1 row of a tile: G, the packed X rows, per-point terms,
+// output staging (two buffers) and the r1 operands of the int_2e contraction.
 static size_t r1_row_bytes(const Request &R)
 {
-    size_t g = 4 * (size_t)R.n2 * sizeof(double);
-    if (R.precision == CUTC_SPLIT_BF16)
-        g += split_r1_row_bytes(R);
-    return g;
+    const int64_t np = n_pairs(R.nA), nl = std::max<int64_t>(1, n_strict_pairs(R.nA));
+    size_t b = 4 * (size_t)R.n2 * 8 + 4 * (size_t)np * 8 + (size_t)R.nN * sizeof(NucTerm);
+    if (!(R.device_pointers || R.out_device))
+        b += 2 * (size_t)R.x_components * R.nA * R.nA * 8;
+    if (R.precision == CUTC_PLAIN_FP64)
+        b += ((size_t)np + 3 * (size_t)nl) * 8;
+    else
+        b += split_r1_row_bytes(R) + pair_df_poly_bytes(6, 1, R.nN);
+    return b;
 }
 
 size_t build_footprint(const Request &R, size_t tile_budget)
 {
     const int64_t n1 = R.n1, n2 = R.n2, nA = R.nA, nN = R.nN;
-    const int64_t np = n_pairs(nA), nl = std::max<int64_t>(1, n_strict_pairs(nA)), nA2 = nA * nA;
-    const int64_t n1t = std::max<int64_t>(1, std::min<int64_t>(n1, (int64_t)(tile_budget / r1_row_bytes(R))));
-    auto up = [](int64_t a, int64_t b) { return (a + b - 1) / b * b; };
-    double b = 0;
-    b += 4.0 * n1t * n2 * 8 + (double)n1t * nN * sizeof(NucTerm) + (double)nN * n2 * 8;
-    b += 4.0 * n1 * np * 8;
-    if (!(R.device_pointers || R.out_device))
-        b += ((double)R.x_components * n1 * nA2 + (double)nA2 * nA2) * 8;
+    const size_t row = r1_row_bytes(R);
+    const int64_t n1t = std::max<int64_t>(1, std::min<int64_t>(n1, (int64_t)(tile_budget / row)));
+    double b = (double)fixed_bytes(R) + (double)n1t * row;
     if (!(R.device_pointers || R.in_device))
         b += (4.0 * n1 + 4.0 * n2 + 3.0 * nN + 4.0 * n1 * nA + (double)n2 * nA) * 8;
-    if (R.precision == CUTC_PLAIN_FP64) {
-        b += ((double)np * n2 + (double)np * n1 + 3.0 * nl * n1 + (double)np * np + (double)np * nl) * 8;
-    } else {
-        const double S2 = 2.0 * R.n_slices;
-        b += S2 * up(np, 128) * up(n2, 32) + S2 * up(4 * n1t, 48) * up(n2, 32);
-        b += S2 * (up(np, 128) * up(n1, 32) + up(np, 128) * up(3 * n1, 32) + up(np, 48) * up(n1, 32) +
-                   up(nl, 48) * up(3 * n1, 32));
-        b += ((double)np * np + (double)np * nl) * 8 + (4.0 * n2 + nN * n2) * 8 + n1t * nN * 91.0 * 8;
-    }
     return (size_t)(b * 1.05) + ((size_t)64 << 20);
 }
+
+// Waits for the build's copies and kernels on every exit path, so that no copy
+// into the caller's arrays is still running when the call returns.
+struct StreamsDrain {
+    cudaStream_t a, b;
+    ~StreamsDrain()
+    {
+        cudaStreamSynchronize(b);
+        cudaStreamSynchronize(a);
+    }
+};
 
 int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
 {
@@ -350,7 +385,6 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
 
     // ---- inputs on the device --------------------------------------------
     const double *d_r1, *d_wr1, *d_r2, *d_wr2, *d_rn, *d_aos1, *d_aos2v;
-    double *d_X, *d_I;
     void *p;
     auto put = [&](int slot, const void *h, size_t bytes, const double **dst) -> int {
         CUTC_TRY(W.get(slot, bytes, &p));
@@ -374,15 +408,6 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         // only the value component of aos_data2 is used (src/long_range_integ.cu:30-35)
         CUTC_TRY(put(S_AOS2, R.aos2, (size_t)n2 * nA * 8, &d_aos2v));
     }
-    if (out_dev) {
-        d_X = R.X;
-        d_I = R.I;
-    } else {
-        CUTC_TRY(W.get(S_XOUT, (size_t)R.x_components * n1 * nA2 * 8, &p));
-        d_X = (double *)p;
-        CUTC_TRY(W.get(S_IOUT, (size_t)nA2 * nA2 * 8, &p));
-        d_I = (double *)p;
-    }
     const int nt = (int)exps.size();
     double *d_coef;
     int *d_exps, *d_off;
@@ -400,37 +425,64 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[1], st));
 
     // ---- r1 tiling ---------------------------------------------------------
+    // Every r1 tile is carried all the way: pair terms, its X rows (written
+    // out), and its share of the int_2e contractions, accumulated in FP64 in
+    // H and N.  Device memory is the fixed part plus one tile.
+    const size_t row_bytes = r1_row_bytes(R);
     size_t budget = R.max_work_bytes;
     if (budget == 0) {
         size_t free_b = 0, total_b = 0;
         CUTC_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
         budget = std::min<size_t>((size_t)24 << 30, free_b / 3);
+        const size_t fixed = fixed_bytes(R);
+        if (free_b > fixed)
+            budget = std::min<size_t>(budget, (size_t)((double)(free_b - fixed) * 0.8));
     }
-    int64_t n1t = (int64_t)(budget / r1_row_bytes(R));
+    int64_t n1t = (int64_t)(budget / row_bytes);
     n1t = std::max<int64_t>(1, std::min<int64_t>(n1t, n1));
     if (R.tile_rows > 0)
         n1t = std::min<int64_t>(n1t, R.tile_rows);
     const int n_tiles = (int)((n1 + n1t - 1) / n1t);
-
+    constexpr int kTileEv = 6;
     if (stats) {
-        while ((int)E->tile_ev.size() < 4 * n_tiles) {
+        while ((int)E->tile_ev.size() < kTileEv * n_tiles) {
             cudaEvent_t e;
             CUTC_CUDA_TRY(cudaEventCreate(&e));
             E->tile_ev.push_back(e);
         }
     }
 
-    // ---- per-point and pair-product terms -----------------------------------
+    // ---- buffers -------------------------------------------------------------
     NucTerm *d_t1;
-    double *d_f2, *d_P, *d_G, *d_Xp;
+    double *d_f2, *d_P = nullptr, *d_G, *d_Xt, *d_H, *d_N, *d_S0 = nullptr, *d_Sl = nullptr;
+    double *stage_x[2] = {nullptr, nullptr}, *stage_i[2] = {nullptr, nullptr};
     CUTC_TRY(W.get(S_T1, (size_t)n1t * nN * sizeof(NucTerm), &p));
     d_t1 = (NucTerm *)p;
     CUTC_TRY(W.get(S_F2, (size_t)nN * n2 * 8, &p));
     d_f2 = (double *)p;
     CUTC_TRY(W.get(S_G, 4 * (size_t)n1t * n2 * 8, &p));
     d_G = (double *)p;
-    CUTC_TRY(W.get(S_XP, 4 * (size_t)n1 * np * 8, &p));
-    d_Xp = (double *)p;
+    CUTC_TRY(W.get(S_XP, 4 * (size_t)n1t * np * 8, &p));
+    d_Xt = (double *)p;
+    CUTC_TRY(W.get(S_H, (size_t)np * np * 8, &p));
+    d_H = (double *)p;
+    CUTC_TRY(W.get(S_N, (size_t)np * std::max<int64_t>(nl, 1) * 8, &p));
+    d_N = (double *)p;
+    const int slab = int2e_slab_cols(nA);
+    if (!out_dev) {
+        for (int k = 0; k < 2; k++) {
+            CUTC_TRY(W.get(S_XOUT + k, (size_t)R.x_components * n1t * nA2 * 8, &p));
+            stage_x[k] = (double *)p;
+            CUTC_TRY(W.get(S_IOUT + k, (size_t)slab * nA2 * 8, &p));
+            stage_i[k] = (double *)p;
+        }
+    }
+    if (R.precision == CUTC_PLAIN_FP64) {
+        CUTC_TRY(W.get(S_S0, (size_t)np * n1t * 8, &p));
+        d_S0 = (double *)p;
+        CUTC_TRY(W.get(S_SL, (size_t)std::max<int64_t>(nl, 1) * 3 * n1t * 8, &p));
+        d_Sl = (double *)p;
+    }
     CUTC_TRY(launch_r2_terms(st, n2, nN, d_r2, d_rn, R.a_en, d_f2));
     note_launches(1);
 
@@ -462,12 +514,30 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     }
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[2], st));
 
-    // ---- X build, tile by tile ------------------------------------------------
+    // ---- tiles ---------------------------------------------------------------
+    // Host outputs leave through two staging buffers on the transfer stream; the
+    // copy of a tile is issued after the next tile is queued, so a copy into
+    // pageable memory (which holds the calling thread) overlaps device work.
+    StreamsDrain drain{st, E->xfer};
+    cudaEvent_t ready[2] = {E->ev[3], E->ev[4]}, done[2] = {E->ev[9], E->ev[10]};
+    bool busy[2] = {false, false};
+    auto copy_x = [&](int tile) -> int {
+        const int b = tile & 1;
+        const int64_t i0 = (int64_t)tile * n1t, nb = std::min<int64_t>(n1t, n1 - i0);
+        CUTC_CUDA_TRY(cudaStreamWaitEvent(E->xfer, ready[b], 0));
+        for (int m = 0; m < R.x_components; m++)
+            CUTC_CUDA_TRY(cudaMemcpyAsync(R.X + ((int64_t)m * n1 + i0) * nA2,
+                                          stage_x[b] + (int64_t)m * nb * nA2,
+                                          (size_t)nb * nA2 * 8, cudaMemcpyDeviceToHost, E->xfer));
+        CUTC_CUDA_TRY(cudaEventRecord(done[b], E->xfer));
+        busy[b] = true;
+        return CUTC_OK;
+    };
     CUBLAS_TRY(cublasSetStream(E->blas, st));
     for (int tile = 0; tile < n_tiles; tile++) {
         const int i0 = (int)(tile * n1t);
         const int nb = (int)std::min<int64_t>(n1t, n1 - i0);
-        cudaEvent_t *tev = stats ? &E->tile_ev[4 * tile] : nullptr;
+        cudaEvent_t *tev = stats ? &E->tile_ev[kTileEv * tile] : nullptr;
         CUTC_TRY(launch_r1_terms(st, i0, nb, nN, d_r1, d_rn, R.a_en, d_t1));
         if (tev)
             CUTC_CUDA_TRY(cudaEventRecord(tev[0], st));
@@ -500,82 +570,130 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         }
         if (tev)
             CUTC_CUDA_TRY(cudaEventRecord(tev[1], st));
+
+        // X rows of the tile: Xt[(m nb + i) np + p] = sum_g P[p n2 + g] G[m plane + i n2 + g]
         if (R.precision == CUTC_PLAIN_FP64) {
-            // Xp[(m n1 + i0 + i) np + p] = sum_g P[p n2 + g] G[m plane + i n2 + g]
             const double one = 1.0, zero = 0.0;
             if (tev)
                 CUTC_CUDA_TRY(cudaEventRecord(tev[2], st));
             CUBLAS_TRY(cublasDgemmStridedBatched(
                 E->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)np, nb, n2, &one, d_P, n2, 0, d_G, n2,
-                (long long)nb * n2, &zero, d_Xp + (int64_t)i0 * np, (int)np,
-                (long long)n1 * np, 4));
+                (long long)nb * n2, &zero, d_Xt, (int)np, (long long)nb * np, 4));
             if (tev)
                 CUTC_CUDA_TRY(cudaEventRecord(tev[3], st));
         } else {
-            CUTC_TRY(split_x_tile(E, R, st, sp, reinterpret_cast<const float2 *>(d_G), i0, nb, d_Xp,
+            CUTC_TRY(split_x_tile(E, R, st, sp, reinterpret_cast<const float2 *>(d_G), nb, d_Xt,
                                   tev ? tev[2] : nullptr, tev ? tev[3] : nullptr));
         }
+
+        // the tile's share of int_2e (src/build_int_2e_ao.cu:60-67 and 97-104, packed):
+        //   H += X_3 S0,   N += -1/2 [X_0 X_1 X_2] S   over the tile's r1 points
+        if (tev)
+            CUTC_CUDA_TRY(cudaEventRecord(tev[4], st));
+        if (R.precision == CUTC_PLAIN_FP64) {
+            const bool keep = nb == n1 && R.mol_tag && E->tag_i == R.mol_tag && E->tag_i_buf == d_S0;
+            if (!keep) {
+                CUTC_TRY(launch_sym_products(st, nb, nA, d_wr1 + i0, d_aos1 + i0, n1, d_S0, nb));
+                CUTC_TRY(launch_antisym_products(st, nb, nA, d_wr1 + i0, d_aos1 + i0, n1, d_Sl,
+                                                 3 * (int64_t)nb));
+                note_launches(2);
+            }
+            E->tag_i = nb == n1 ? R.mol_tag : 0;
+            E->tag_i_buf = d_S0;
+            const double one = 1.0, mhalf = -0.5, beta = tile == 0 ? 0.0 : 1.0;
+            CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)np, nb, &one,
+                                   d_Xt + 3 * (int64_t)nb * np, (int)np, d_S0, nb, &beta, d_H,
+                                   (int)np));
+            if (nl > 0)
+                CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)nl, 3 * nb,
+                                       &mhalf, d_Xt, (int)np, d_Sl, 3 * nb, &beta, d_N, (int)np));
+        } else {
+            CUTC_TRY(split_int2e_tile(E, R, st, sp, d_wr1 + i0, d_aos1 + i0, n1, nb, d_Xt, d_H,
+                                      d_N, tile == 0));
+        }
+        if (tev)
+            CUTC_CUDA_TRY(cudaEventRecord(tev[5], st));
+
+        // the tile's X rows in the reference layout X[m][i][b][a]
+        if (out_dev) {
+            for (int m = 0; m < R.x_components; m++)
+                CUTC_TRY(launch_expand_pairs(st, nb, nA, d_Xt + (int64_t)m * nb * np, np,
+                                             R.X + ((int64_t)m * n1 + i0) * nA2));
+        } else {
+            const int b = tile & 1;
+            if (busy[b])
+                CUTC_CUDA_TRY(cudaStreamWaitEvent(st, done[b], 0));
+            CUTC_TRY(launch_expand_pairs(st, (int64_t)R.x_components * nb, nA, d_Xt, np, stage_x[b]));
+            CUTC_CUDA_TRY(cudaEventRecord(ready[b], st));
+            if (tile > 0)
+                CUTC_TRY(copy_x(tile - 1));
+        }
+        note_launches(out_dev ? R.x_components : 1);
     }
+    if (!out_dev && n_tiles > 0)
+        CUTC_TRY(copy_x(n_tiles - 1));
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[5], st));
 
-    // ---- int_2e -------------------------------------------------------------
-    if (R.precision == CUTC_PLAIN_FP64) {
-        double *d_S0, *d_Sl, *d_H, *d_N;
-        CUTC_TRY(W.get(S_S0, (size_t)np * n1 * 8, &p));
-        d_S0 = (double *)p;
-        CUTC_TRY(W.get(S_SL, (size_t)std::max<int64_t>(nl, 1) * 3 * n1 * 8, &p));
-        d_Sl = (double *)p;
-        CUTC_TRY(W.get(S_H, (size_t)np * np * 8, &p));
-        d_H = (double *)p;
-        CUTC_TRY(W.get(S_N, (size_t)np * std::max<int64_t>(nl, 1) * 8, &p));
-        d_N = (double *)p;
-        if (!(R.mol_tag && E->tag_i == R.mol_tag && E->tag_i_buf == d_S0)) {
-            CUTC_TRY(launch_sym_products(st, n1, nA, d_wr1, d_aos1, n1, d_S0, n1));
-            CUTC_TRY(launch_antisym_products(st, n1, nA, d_wr1, d_aos1, d_Sl, 3 * (int64_t)n1));
-            note_launches(2);
-            E->tag_i = R.mol_tag;
-            E->tag_i_buf = d_S0;
-        }
-        const double one = 1.0, zero = 0.0, mhalf = -0.5;
-        // H = X_3 S0   (src/build_int_2e_ao.cu:60-67, packed)
-        CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)np, n1, &one,
-                               d_Xp + 3 * (int64_t)n1 * np, (int)np, d_S0, n1, &zero, d_H, (int)np));
-        // N = -1/2 [X_0 X_1 X_2] S   (src/build_int_2e_ao.cu:97-104, packed)
-        if (nl > 0)
-            CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)nl, 3 * n1,
-                                   &mhalf, d_Xp, (int)np, d_Sl, 3 * n1, &zero, d_N, (int)np));
-        CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, d_I));
+    // ---- int_2e = A + A^T ------------------------------------------------------
+    if (out_dev) {
+        CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, 0, (int)nA2, R.I));
         note_launches(1);
     } else {
-        CUTC_TRY(split_int2e(E, R, st, sp, d_wr1, d_aos1, d_Xp, d_I));
+        // column slabs: assemble slab s while slab s - 1 is copied out
+        const int n_slabs = (int)((nA2 + slab - 1) / slab);
+        bool ibusy[2] = {false, false};
+        auto copy_i = [&](int slab_no) -> int {
+            const int b = slab_no & 1;
+            const int64_t c0 = (int64_t)slab_no * slab, c1 = std::min<int64_t>(nA2, c0 + slab);
+            CUTC_CUDA_TRY(cudaStreamWaitEvent(E->xfer, ready[b], 0));
+            CUTC_CUDA_TRY(cudaMemcpyAsync(R.I + c0 * nA2, stage_i[b], (size_t)(c1 - c0) * nA2 * 8,
+                                          cudaMemcpyDeviceToHost, E->xfer));
+            CUTC_CUDA_TRY(cudaEventRecord(done[b], E->xfer));
+            ibusy[b] = true;
+            return CUTC_OK;
+        };
+        // the X copies still pending on the staging events must be waited for
+        // before those events are recorded again
+        for (int b = 0; b < 2; b++)
+            if (busy[b])
+                CUTC_CUDA_TRY(cudaStreamWaitEvent(st, done[b], 0));
+        for (int sl = 0; sl < n_slabs; sl++) {
+            const int b = sl & 1;
+            const int c0 = sl * slab, c1 = (int)std::min<int64_t>(nA2, (int64_t)c0 + slab);
+            if (ibusy[b])
+                CUTC_CUDA_TRY(cudaStreamWaitEvent(st, done[b], 0));
+            CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, c0, c1, stage_i[b]));
+            note_launches(1);
+            CUTC_CUDA_TRY(cudaEventRecord(ready[b], st));
+            if (sl > 0)
+                CUTC_TRY(copy_i(sl - 1));
+        }
+        CUTC_TRY(copy_i(n_slabs - 1));
     }
-    CUTC_CUDA_TRY(cudaEventRecord(E->ev[6], st));
-
-    // ---- X in the reference layout, outputs to the host -------------------------
-    CUTC_TRY(launch_expand_pairs(st, (int64_t)R.x_components * n1, nA, d_Xp, np, d_X));
-    note_launches(1);
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[7], st));
-    if (!out_dev) {
-        CUTC_CUDA_TRY(cudaMemcpyAsync(R.X, d_X, (size_t)R.x_components * n1 * nA2 * 8,
-                                      cudaMemcpyDeviceToHost, st));
-        CUTC_CUDA_TRY(cudaMemcpyAsync(R.I, d_I, (size_t)nA2 * nA2 * 8, cudaMemcpyDeviceToHost, st));
-    }
+    CUTC_CUDA_TRY(cudaEventRecord(E->ev[11], E->xfer));
+    CUTC_CUDA_TRY(cudaStreamWaitEvent(st, E->ev[11], 0));
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[8], st));
     CUTC_CUDA_TRY(cudaEventSynchronize(E->ev[8]));
     CUTC_CUDA_TRY(cudaGetLastError());
+    if (R.precision == CUTC_SPLIT_BF16)
+        CUTC_TRY(split_check(st, sp));
 
     if (stats) {
-        double ms_pair = 0.0, ms_gemm = 0.0;
+        double ms_pair = 0.0, ms_gemm = 0.0, ms_i = 0.0, ms_tiles = 0.0;
         for (int t = 0; t < n_tiles; t++) {
-            ms_pair += ev_ms(E->tile_ev[4 * t], E->tile_ev[4 * t + 1]);
-            ms_gemm += ev_ms(E->tile_ev[4 * t + 2], E->tile_ev[4 * t + 3]);
+            const cudaEvent_t *e = &E->tile_ev[kTileEv * t];
+            ms_pair += ev_ms(e[0], e[1]);
+            ms_gemm += ev_ms(e[2], e[3]);
+            ms_i += ev_ms(e[4], e[5]);
+            ms_tiles += ev_ms(e[0], e[5]);
         }
         stats->ms_x_gemm = ms_gemm;
         stats->n_x_gemm = n_tiles;
         stats->ms_h2d = ev_ms(E->ev[0], E->ev[1]);
         stats->ms_pair = ms_pair;
-        stats->ms_x = ev_ms(E->ev[1], E->ev[5]) - ms_pair;
-        stats->ms_int2e = ev_ms(E->ev[5], E->ev[6]);
+        stats->ms_x = ev_ms(E->ev[1], E->ev[2]) + ms_tiles - ms_pair - ms_i;
+        stats->ms_int2e = ms_i + ev_ms(E->ev[5], E->ev[7]);
         stats->ms_d2h = ev_ms(E->ev[7], E->ev[8]);
         stats->ms_total = ev_ms(E->ev[0], E->ev[8]);
         stats->n_r1_tiles = n_tiles;

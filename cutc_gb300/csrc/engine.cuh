@@ -30,6 +30,7 @@ struct Engine {
     int max_threads_per_block = 1024;
     int max_grid[3] = {0, 0, 0};
     cudaStream_t stream = nullptr;
+    cudaStream_t xfer = nullptr;  // device-to-host copies of finished r1 tiles
     cublasHandle_t blas = nullptr;
     cudaEvent_t ev[kNumEvents];
     std::vector<cudaEvent_t> tile_ev;  // per-tile timing events (grown on demand)

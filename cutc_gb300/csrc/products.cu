@@ -32,27 +32,28 @@ __global__ void sym_products_kernel(int n, int nA, const double *__restrict__ w,
 }
 
 // out[stri(c, d) * ld + m * n + g] = w (chi_c d_m chi_d - chi_d d_m chi_c), c > d
-// aos is the (n, nA, 4) array; component k of AO a at aos[(k * nA + a) * n + g].
+// aos is the (ld_aos, nA, 4) array seen from the first of the n grid points;
+// component k of AO a at aos[(k * nA + a) * ld_aos + g].
 __global__ void antisym_products_kernel(int n, int nA, const double *__restrict__ w,
-                                        const double *__restrict__ aos,
+                                        const double *__restrict__ aos, int64_t ld_aos,
                                         double *__restrict__ out, int64_t ld)
 {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = blockIdx.y;
     if (g >= n)
         return;
-    const int64_t comp = (int64_t)nA * n;
+    const int64_t comp = (int64_t)nA * ld_aos;
     const double wg = w[g];
-    const double vc = aos[(int64_t)c * n + g];
-    const double dc0 = aos[comp + (int64_t)c * n + g];
-    const double dc1 = aos[2 * comp + (int64_t)c * n + g];
-    const double dc2 = aos[3 * comp + (int64_t)c * n + g];
+    const double vc = aos[(int64_t)c * ld_aos + g];
+    const double dc0 = aos[comp + (int64_t)c * ld_aos + g];
+    const double dc1 = aos[2 * comp + (int64_t)c * ld_aos + g];
+    const double dc2 = aos[3 * comp + (int64_t)c * ld_aos + g];
     for (int d = 0; d < c; d++) {
-        const double vd = aos[(int64_t)d * n + g];
+        const double vd = aos[(int64_t)d * ld_aos + g];
         double *o = out + stri_index(c, d, nA) * ld + g;
-        o[0] = wg * (vc * aos[comp + (int64_t)d * n + g] - vd * dc0);
-        o[n] = wg * (vc * aos[2 * comp + (int64_t)d * n + g] - vd * dc1);
-        o[2 * (int64_t)n] = wg * (vc * aos[3 * comp + (int64_t)d * n + g] - vd * dc2);
+        o[0] = wg * (vc * aos[comp + (int64_t)d * ld_aos + g] - vd * dc0);
+        o[n] = wg * (vc * aos[2 * comp + (int64_t)d * ld_aos + g] - vd * dc1);
+        o[2 * (int64_t)n] = wg * (vc * aos[3 * comp + (int64_t)d * ld_aos + g] - vd * dc2);
     }
 }
 
@@ -92,31 +93,33 @@ __device__ __forceinline__ double a_entry(int row, int col, int nA, int64_t np,
     return v;
 }
 
-// out[row + n col] = A[row, col] + A[col, row], n = nA^2, 32x32 tiles
+// out[row + n (col - c0)] = A[row, col] + A[col, row] for the columns
+// c0 <= col < c1, n = nA^2, 32x32 tiles
 __global__ void assemble_int2e_kernel(int nA, const double *__restrict__ H,
-                                      const double *__restrict__ N, double *__restrict__ out)
+                                      const double *__restrict__ N, int c0, int c1,
+                                      double *__restrict__ out)
 {
     __shared__ double t[32][33];
     const int n = nA * nA;
     const int64_t np = (int64_t)nA * (nA + 1) / 2;
-    const int R0 = blockIdx.x * 32, C0 = blockIdx.y * 32;
+    const int R0 = blockIdx.x * 32, C0 = c0 + blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
     double v[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         const int row = R0 + tx, col = C0 + ty + 8 * k;
-        v[k] = (row < n && col < n) ? a_entry(row, col, nA, np, H, N) : 0.0;
+        v[k] = (row < n && col < c1) ? a_entry(row, col, nA, np, H, N) : 0.0;
         // transposed term, computed with tx running along A's row index
         const int row2 = C0 + tx, col2 = R0 + ty + 8 * k;
-        t[ty + 8 * k][tx] = (row2 < n && col2 < n) ? a_entry(row2, col2, nA, np, H, N) : 0.0;
+        t[ty + 8 * k][tx] = (row2 < c1 && col2 < n) ? a_entry(row2, col2, nA, np, H, N) : 0.0;
     }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         const int row = R0 + tx, col = C0 + ty + 8 * k;
         // t[i][j] = A[C0 + j, R0 + i]  ->  A[col, row] = t[tx][ty + 8k]
-        if (row < n && col < n)
-            out[row + (int64_t)n * col] = v[k] + t[tx][ty + 8 * k];
+        if (row < n && col < c1)
+            out[row + (int64_t)n * (col - c0)] = v[k] + t[tx][ty + 8 * k];
     }
 }
 
@@ -132,12 +135,12 @@ int launch_sym_products(cudaStream_t st, int n, int nA, const double *w, const d
 }
 
 int launch_antisym_products(cudaStream_t st, int n, int nA, const double *w, const double *aos,
-                            double *out, int64_t ld)
+                            int64_t ld_aos, double *out, int64_t ld)
 {
     if (n <= 0 || nA < 2)
         return CUTC_OK;
     dim3 grid(ceil_div(n, 128), nA);
-    antisym_products_kernel<<<grid, 128, 0, st>>>(n, nA, w, aos, out, ld);
+    antisym_products_kernel<<<grid, 128, 0, st>>>(n, nA, w, aos, ld_aos, out, ld);
     CUTC_CUDA_TRY(cudaGetLastError());
     return CUTC_OK;
 }
@@ -158,11 +161,14 @@ int launch_expand_pairs(cudaStream_t st, int64_t rows, int nA, const double *Xp,
     return CUTC_OK;
 }
 
-int launch_assemble_int2e(cudaStream_t st, int nA, const double *H, const double *N, double *out)
+int launch_assemble_int2e(cudaStream_t st, int nA, const double *H, const double *N, int c0,
+                          int c1, double *out)
 {
     const int n = nA * nA;
-    dim3 grid(ceil_div(n, 32), ceil_div(n, 32));
-    assemble_int2e_kernel<<<grid, dim3(32, 8), 0, st>>>(nA, H, N, out);
+    if (c0 < 0 || c1 > n || c0 >= c1)
+        return CUTC_OK;
+    dim3 grid(ceil_div(n, 32), ceil_div(c1 - c0, 32));
+    assemble_int2e_kernel<<<grid, dim3(32, 8), 0, st>>>(nA, H, N, c0, c1, out);
     CUTC_CUDA_TRY(cudaGetLastError());
     return CUTC_OK;
 }

@@ -370,16 +370,17 @@ struct SrcSym {  // w[k] chi_a(k) chi_b(k), (a, b) = pairs[r]
 };
 
 struct SrcAnti {  // w (chi_c d_m chi_d - chi_d d_m chi_c), k = m n + g, (c, d) = pairs[r]
-    const double *w, *aos;
-    int n, nA;
+    const double *w, *aos;  // aos: (ld, nA, 4) with the grid offset already applied
+    int n, nA;              // n: grid points counted in k (g < n)
+    int64_t ld;             // grid stride of aos
     const int2 *pairs;
     __device__ double operator()(int64_t r, int64_t k) const
     {
         const int m = (int)(k / n), g = (int)(k % n);
         const int2 cd = pairs[r];
-        const int64_t comp = (int64_t)nA * n * (m + 1);
-        const double vc = aos[(int64_t)cd.x * n + g], vd = aos[(int64_t)cd.y * n + g];
-        return w[g] * (vc * aos[comp + (int64_t)cd.y * n + g] - vd * aos[comp + (int64_t)cd.x * n + g]);
+        const int64_t comp = (int64_t)nA * ld * (m + 1);
+        const double vc = aos[cd.x * ld + g], vd = aos[cd.y * ld + g];
+        return w[g] * (vc * aos[comp + cd.y * ld + g] - vd * aos[comp + cd.x * ld + g]);
     }
 };
 
@@ -692,14 +693,24 @@ static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alph
 
 enum SplitSlot {
     SS_PAIRS_SYM = 0, SS_PAIRS_ANTI = 1, SS_ERR = 2,
-    SS_AX = 3, SS_BX = 6, SS_AH = 9, SS_AN = 12, SS_BH = 15, SS_BN = 18, SS_H = 21, SS_N = 22,
+    SS_AX = 3, SS_BX = 6, SS_AH = 9, SS_AN = 12, SS_BH = 15, SS_BN = 18,
 };
 
 
 size_t split_r1_row_bytes(const Request &R)
 {
-    // BF16 slices of the four G rows of one r1 point
-    return 4 * (size_t)R.n_slices * round_up(R.n2, kBK) * 2;
+    const int64_t np = n_pairs(R.nA), nl = std::max<int64_t>(1, n_strict_pairs(R.nA));
+    const int bn = bn_for(R.n_slices);
+    const size_t S2 = 2 * (size_t)R.n_slices;
+    // slices of the four G rows of one r1 point, plus the point's K columns of the
+    // int_2e operands (X_3, X_012, S0, S)
+    return S2 * (4 * (size_t)round_up(R.n2, kBK) + round_up(np, kBM) * 4 + round_up(np, bn) +
+                 3 * (size_t)round_up(nl, bn)) + 64;
+}
+
+size_t split_fixed_bytes(const Request &R)
+{
+    return 2 * (size_t)R.n_slices * round_up(n_pairs(R.nA), kBM) * round_up(R.n2, kBK);
 }
 
 static int upload_pairs(Workspace &W, int slot, cudaStream_t st, int nA, bool strict, int2 **out)
@@ -757,7 +768,7 @@ int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *
 }
 
 int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const float2 *G,
-                 int i0, int nb, double *Xp, cudaEvent_t gemm_begin, cudaEvent_t gemm_end)
+                 int nb, double *Xt, cudaEvent_t gemm_begin, cudaEvent_t gemm_end)
 {
     (void)E;
     SplitPlan &S_ = sp;
@@ -770,54 +781,61 @@ int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, co
         CUTC_TRY((slice_rows<S, SrcDenseDF>(st, src, B)));
         if (gemm_begin)
             CUTC_CUDA_TRY(cudaEventRecord(gemm_begin, st));
-        CUTC_TRY((gemm<S>(st, S_.AX, B, 1.0, Xp, np, nb, R.n1, i0, 0, S_.err, R.k_split)));
+        CUTC_TRY((gemm<S>(st, S_.AX, B, 1.0, Xt, np, B.M, 0, 0, 0, S_.err, R.k_split)));
         if (gemm_end)
             CUTC_CUDA_TRY(cudaEventRecord(gemm_end, st));
     });
     return CUTC_OK;
 }
 
-int split_int2e(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const double *wr1,
-                const double *aos1, const double *Xp, double *I)
+int split_int2e_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
+                     const double *wr1, const double *aos1, int64_t ld1, int nb, const double *Xt,
+                     double *H, double *N, bool first)
 {
     Workspace &W = E->ws;
     SplitPlan &S_ = sp;
     const int slot0 = sp.slot0;
-    const int n1 = R.n1, nA = R.nA;
+    const int nA = R.nA;
     const int np = (int)n_pairs(nA), nl = (int)n_strict_pairs(nA);
-    Operand AH, AN, BH, BN;
-    CUTC_TRY(alloc_operand(W, slot0 + SS_AH, sp.n_slices, np, kBM, n1, AH));
-    CUTC_TRY(alloc_operand(W, slot0 + SS_AN, sp.n_slices, np, kBM, 3 * (int64_t)n1, AN));
     const int bn = bn_for(sp.n_slices);
-    CUTC_TRY(alloc_operand(W, slot0 + SS_BH, sp.n_slices, np, bn, n1, BH));
-    CUTC_TRY(alloc_operand(W, slot0 + SS_BN, sp.n_slices, std::max(nl, 1), bn, 3 * (int64_t)n1, BN));
+    Operand AH, AN, BH, BN;
+    CUTC_TRY(alloc_operand(W, slot0 + SS_AH, sp.n_slices, np, kBM, nb, AH));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_AN, sp.n_slices, np, kBM, 3 * (int64_t)nb, AN));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BH, sp.n_slices, np, bn, nb, BH));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BN, sp.n_slices, std::max(nl, 1), bn, 3 * (int64_t)nb, BN));
     BN.M = nl;
-    void *p;
-    CUTC_TRY(W.get(slot0 + SS_H, (size_t)np * np * 8, &p));
-    double *H = (double *)p;
-    CUTC_TRY(W.get(slot0 + SS_N, (size_t)np * std::max(nl, 1) * 8, &p));
-    double *N = (double *)p;
-    SrcSym s0{wr1, aos1, (int64_t)n1, S_.pairs_sym};
-    SrcAnti sa{wr1, aos1, n1, nA, S_.pairs_anti};
-    const bool reuse_b = R.mol_tag && E->tag_i == R.mol_tag && E->tag_i_buf == BH.sl;
+    SrcSym s0{wr1, aos1, ld1, S_.pairs_sym};
+    SrcAnti sa{wr1, aos1, nb, nA, ld1, S_.pairs_anti};
+    const int acc = first ? 0 : 1;
+    // With the whole r1 grid in one tile the B operands depend on the molecule
+    // only, and a build with the same molecule tag keeps them.
+    const bool keep_b = nb == R.n1 && R.mol_tag && E->tag_i == R.mol_tag && E->tag_i_buf == BH.sl;
     CUTC_SLICES_DISPATCH(sp.n_slices, {
-        CUTC_TRY(slice_cols<S>(st, Xp, np, 3 * (int64_t)n1, AH));
-        CUTC_TRY(slice_cols<S>(st, Xp, np, 0, AN));
-        if (!reuse_b)
+        // Xt[(m nb + i) np + p]: X_3 is column block 3, X_012 the blocks 0..2
+        CUTC_TRY(slice_cols<S>(st, Xt, np, 3 * (int64_t)nb, AH));
+        CUTC_TRY(slice_cols<S>(st, Xt, np, 0, AN));
+        if (!keep_b) {
             CUTC_TRY((slice_rows<S, SrcSym>(st, s0, BH)));
-        CUTC_TRY(gemm<S>(st, AH, BH, 1.0, H, np, np, 0, 0, 0, S_.err, R.k_split));
-        if (nl > 0) {
-            if (!reuse_b)
+            if (nl > 0)
                 CUTC_TRY((slice_rows<S, SrcAnti>(st, sa, BN)));
-            CUTC_TRY(gemm<S>(st, AN, BN, -0.5, N, np, nl, 0, 0, 0, S_.err, R.k_split));
         }
+        CUTC_TRY(gemm<S>(st, AH, BH, 1.0, H, np, np, 0, 0, acc, S_.err, R.k_split));
+        if (nl > 0)
+            CUTC_TRY(gemm<S>(st, AN, BN, -0.5, N, np, nl, 0, 0, acc, S_.err, R.k_split));
     });
-    E->tag_i = R.mol_tag;
-    E->tag_i_buf = BH.sl;
-    CUTC_TRY(launch_assemble_int2e(st, nA, H, N, I));
-    note_launches(1);
+    if (nb == R.n1) {
+        E->tag_i = R.mol_tag;
+        E->tag_i_buf = BH.sl;
+    } else {
+        E->tag_i = 0;
+    }
+    return CUTC_OK;
+}
+
+int split_check(cudaStream_t st, SplitPlan &sp)
+{
     int herr = 0;
-    CUTC_CUDA_TRY(cudaMemcpyAsync(&herr, S_.err, 4, cudaMemcpyDeviceToHost, st));
+    CUTC_CUDA_TRY(cudaMemcpyAsync(&herr, sp.err, 4, cudaMemcpyDeviceToHost, st));
     CUTC_CUDA_TRY(cudaStreamSynchronize(st));
     if (herr) {
         cutc_set_error(CUTC_ERR_TIMEOUT, "a tensor-core pipeline wait gave up (code %d)", herr);

@@ -31,14 +31,22 @@ struct SplitPlan {
     int *err = nullptr;                // device flag set by a bounded wait that gave up
 };
 
+// Device bytes per r1 row of a tile (slices of G and of the tile's int_2e operands).
 size_t split_r1_row_bytes(const Request &R);
+// Device bytes that do not depend on the tile size (the P slices).
+size_t split_fixed_bytes(const Request &R);
 int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *wr2,
                     const double *aos2v, int64_t n1t, int slot0, SplitPlan &sp);
-// G is the df tile G[c][i][j] as (hi, lo) float pairs
+// X of one r1 tile: Xt[(m nb + i) np + p] from the df tile G[c][i][j] ((hi, lo) pairs).
 int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const float2 *G,
-                 int i0, int nb, double *Xp, cudaEvent_t gemm_begin, cudaEvent_t gemm_end);
-int split_int2e(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const double *wr1,
-                const double *aos1, const double *Xp, double *I);
+                 int nb, double *Xt, cudaEvent_t gemm_begin, cudaEvent_t gemm_end);
+// Adds the r1 tile's share of the int_2e contractions to H and N (overwrites when
+// first): wr1 and aos1 point at the tile's first row, ld1 is the row stride of aos1.
+int split_int2e_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
+                     const double *wr1, const double *aos1, int64_t ld1, int nb, const double *Xt,
+                     double *H, double *N, bool first);
+// Reports a bounded wait that gave up in any of the launches (synchronises).
+int split_check(cudaStream_t st, SplitPlan &sp);
 // C[m + ldc n] = sum_k A[m K + k] B[n K + k] through the split form (device arrays)
 int split_gemm_dense(Engine *E, cudaStream_t st, int n_slices, int M, int N, int64_t K,
                      const double *A, const double *B, double *C, int64_t ldc);

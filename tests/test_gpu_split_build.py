@@ -44,9 +44,11 @@ def test_split_r1_tiling_is_exact():
     X1, I1 = cg.build_integrals(p, cg.SPLIT_BF16)
     X2, I2, st = cg.build_integrals(p, cg.SPLIT_BF16, max_work_bytes=2 << 20, with_stats=True)
     assert st["n_r1_tiles"] > 1
-    # the slices of each G row do not depend on the tile; only the int_2e sum order can
+    # the slices of each G row do not depend on the tile, so X is the same bits;
+    # int_2e is sliced per r1 tile (per-tile row scales), so its split rounding
+    # differs by up to the split tolerance
     assert np.array_equal(X1, X2)
-    assert oracle.rel_err(I2, I1)["max"] < 1e-13
+    assert oracle.rel_err(I2, I1)["max"] < 1e-12
 
 
 def test_split_four_components_and_scale_factors():
