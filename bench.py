@@ -66,6 +66,55 @@ def sub_problem(p, i0, n):
         p, r1=np.ascontiguousarray(p.r1[i0:i0 + n]), wr1=np.ascontiguousarray(p.wr1[i0:i0 + n]),
         aos1=np.ascontiguousarray(p.aos1[:, :, i0:i0 + n]))
 
+def plain_rate_estimate(cg, p, sizes):
+    """Plain FP64 builds/s of the full grid from device-timed builds on two r1
+    samples: T(n) = a + b n fitted through both, evaluated at n_grid1."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    nA2 = p.n_ao ** 2
+    stream = torch.cuda.Stream(device=dev)
+    opt = cg.options(cg.PLAIN_FP64, None, p.a_en, p.a_ee, 3, True, 0, stream.cuda_stream)
+    Id = torch.empty((nA2, nA2), dtype=torch.float64, device=dev)
+    times = []
+    for k, ns in enumerate(sizes):
+        sub = strided_rows(p, ns)
+        dr = {key: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for key, v in sub.arrays().items()}
+        Xd = torch.empty((3, ns, nA2), dtype=torch.float64, device=dev)
+        reps = 2 if k == 0 else 1  # the first build also sets up the workspace
+        for r in range(reps):
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s = cg.cutc_int_ex(opt, ns, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                               dr["r1"], dr["wr1"], dr["r2"], dr["wr2"], dr["rn"], dr["aos1"],
+                               dr["aos2"], dr["c_bh"], dr["m_bh"], dr["n_bh"], dr["o_bh"], Xd, Id, None)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            if s != cg.CUTC_OK:
+                raise cg.CutcError(s, cg.last_error())
+        times.append(e0.elapsed_time(e1))
+        del dr, Xd
+    (n_a, n_b), (t_a, t_b) = sizes, times
+    slope = (t_b - t_a) / (n_b - n_a)
+    t_full = t_b + slope * (p.n_grid1 - n_b)
+    del Id
+    torch.cuda.empty_cache()
+    cg.load().cutc_release()
+    return {"value_est": 1e3 / t_full, "unit": UNIT, "ms_per_build_est": t_full,
+            "basis": "plain FP64 form, device-resident, timed on %d and %d r1 rows (%.0f and %.0f ms) "
+                     "and extrapolated linearly to n_grid1=%d" % (n_a, n_b, t_a, t_b, p.n_grid1)}
+
+
+def strided_rows(p, ns):
+    """The same molecule with ns r1 points spread evenly over the whole r1 grid
+    (every nucleus' shells are represented)."""
+    import dataclasses
+    idx = np.unique(np.linspace(0, p.n_grid1 - 1, ns).round().astype(np.int64))
+    assert len(idx) == ns
+    return dataclasses.replace(
+        p, r1=np.ascontiguousarray(p.r1[idx]), wr1=np.ascontiguousarray(p.wr1[idx]),
+        aos1=np.ascontiguousarray(p.aos1[:, :, idx]))
+
 
 # ---------------------------------------------------------------------------
 # clocks during the timed region
@@ -358,18 +407,13 @@ def run_ours(args):
         rows = 256
         sub = sub_problem(p, (p.n_grid1 // 2) // 64 * 64, rows)
         Xs, Is = cg.build_integrals(sub, cg.SPLIT_BF16, n_slices=args.slices)
-        cg.build_integrals(sub, cg.PLAIN_FP64)
-        t0 = time.perf_counter()
         Xp, Ip = cg.build_integrals(sub, cg.PLAIN_FP64)
-        t_plain = time.perf_counter() - t0
         from oracle.oracle import rel_err
         out["accuracy"] = {"X_vs_fp64": rel_err(Xs, Xp), "int2e_vs_fp64": rel_err(Is, Ip),
                            "sample": "%d of %d r1 rows of the workload; split (%d slices) vs "
                                      "the plain FP64 form (itself 1e-12 from the oracle)"
                                      % (rows, p.n_grid1, args.slices)}
-        out["plain_fp64"] = {"value_est": 1.0 / (t_plain * p.n_grid1 / rows), "unit": UNIT,
-                             "basis": "plain FP64 form on %d r1 rows (host buffers), scaled by "
-                                      "n_grid1/%d" % (rows, rows)}
+        out["plain_fp64"] = plain_rate_estimate(cg, p, (rows, 2 * rows))
     if rank == 0 and world == 1 and not args.skip_cpu:
         log("cpu baseline sample")
         cb, _, _ = cpu_sample(p)
@@ -380,6 +424,179 @@ def run_ours(args):
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+# ---------------------------------------------------------------------------
+# the large workload: r1 samples of the full molecule and grids
+# ---------------------------------------------------------------------------
+def run_large(args):
+    """Large workload (n_ao=300, n_grid2=200,000) timed on two r1 samples spread
+    over the 60,000-point r1 grid and extrapolated linearly in n_grid1.
+
+    A full build's outputs (X: 130 GB, int_2e: 65 GB) do not fit the GPU host's
+    memory beside each other, so the full grid is not built in one call; the
+    device-resident cost of a build is exactly linear in the r1 rows it holds
+    (every r1 tile does the same work), plus a fixed part (P slices, int_2e
+    assembly), which the two samples separate.
+    """
+    import torch
+    import cutc_gb300 as cg
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
+    p = synth.make_config(args.config)
+    nA2 = p.n_ao ** 2
+    sizes = (args.r1_sample // 2, args.r1_sample)
+    stream = torch.cuda.Stream(device=dev)
+    opt = cg.options(prec, args.slices, p.a_en, p.a_ee, 3, True, 0, stream.cuda_stream,
+                     k_split=args.k_split)
+    Id = torch.empty((nA2, nA2), dtype=torch.float64, device=dev)
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        pass
+    samples = []
+    gemm_ms, gemm_launches, launches, pair_ms, flops_x = 0.0, 0, 0, 0.0, 0.0
+    sampler = ClockSampler(uuid)
+    for ns in sizes:
+        sub = strided_rows(p, ns)
+        dr = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in sub.arrays().items()}
+        Xd = torch.empty((3, ns, nA2), dtype=torch.float64, device=dev)
+
+        def build(stats=None):
+            s = cg.cutc_int_ex(opt, ns, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                               dr["r1"], dr["wr1"], dr["r2"], dr["wr2"], dr["rn"], dr["aos1"],
+                               dr["aos2"], dr["c_bh"], dr["m_bh"], dr["n_bh"], dr["o_bh"], Xd, Id,
+                               stats)
+            if s != cg.CUTC_OK:
+                raise cg.CutcError(s, cg.last_error())
+
+        log("large: %d r1 rows, warm-up" % ns)
+        for _ in range(args.warmup):
+            build()
+        if ns == sizes[-1]:
+            sampler.start()
+            time.sleep(0.5)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        tiles = 0
+        for _ in range(args.steps):
+            st = cg.Stats()
+            build(st)
+            tiles = st.n_r1_tiles
+            if ns == sizes[-1]:
+                gemm_ms += st.ms_x_gemm
+                gemm_launches += st.n_x_gemm
+                launches += st.gpu_launches
+                pair_ms += st.ms_pair
+                flops_x += 8.0 * nA2 * ns * p.n_grid2
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / args.steps
+        samples.append({"r1_rows": ns, "ms_per_build": ms, "r1_tiles": tiles})
+        log("large: %d rows: %.1f ms per build" % (ns, ms))
+        del dr, Xd
+    clocks = sampler.stop()
+    del Id
+    torch.cuda.empty_cache()
+    cg.load().cutc_release()
+    (n_a, n_b), (t_a, t_b) = sizes, (samples[0]["ms_per_build"], samples[1]["ms_per_build"])
+    slope = (t_b - t_a) / (n_b - n_a)
+    t_full = t_b + slope * (p.n_grid1 - n_b)
+    value = 1e3 / t_full
+
+    peaks, peak_kind = measured_peaks()
+    peak = float(peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops")))
+    per_launch_ms = gemm_ms / max(1, gemm_launches)
+    achieved = flops_x / max(1, gemm_launches) / (per_launch_ms * 1e-3) / 1e12
+    S = args.slices
+    n_products = S * (S + 1) // 2 if prec == cg.SPLIT_BF16 else 0
+    packed = p.n_ao * (p.n_ao + 1) / 2.0 / nA2
+    executed = achieved * packed * n_products if n_products else None
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_full, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
+           "config": {"workload": workload_desc(args.config, p), "precision": args.precision,
+                      "n_slices": S if prec else None,
+                      "projection": "device-resident builds on %d and %d r1 rows spread over the "
+                                    "r1 grid, extrapolated linearly to n_grid1=%d"
+                                    % (n_a, n_b, p.n_grid1),
+                      "l2": "inputs larger than L2: P slices alone are %.0f GB" %
+                            (2 * S * p.n_ao * (p.n_ao + 1) / 2 * p.n_grid2 / 1e9),
+                      "parallelism": "1 GPU"},
+           "samples": samples, "gpu_launches": launches, "clocks": clocks,
+           "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                        "frac": achieved / peak, "traffic": None,
+                        "kernel": "split_gemm_kernel (X build, one launch per r1 tile)",
+                        "peak_source": "bf16_tflops_sustained of %s" % peak_kind,
+                        "ms_per_launch": per_launch_ms, "executed_bf16_tflops": executed,
+                        "executed_frac": (executed / peak) if executed else None},
+           "phases_ms_per_build_sample": {"pair": pair_ms / args.steps,
+                                          "x_gemm": gemm_ms / args.steps},
+           "e2e": {"value": None, "unit": UNIT,
+                   "reason": "the full build's host outputs (195 GB) exceed the GPU host's memory"}}
+
+    if not args.skip_accuracy:
+        rows = 128
+        log("large: accuracy on %d rows" % rows)
+        sub = strided_rows(p, rows)
+        out["accuracy"] = large_accuracy(cg, sub, args.slices)
+        out["accuracy"]["sample"] = ("%d of %d r1 rows spread over the grid; split (%d slices) vs "
+                                     "the plain FP64 form" % (rows, p.n_grid1, S))
+        log("large: plain FP64 rate")
+        out["plain_fp64"] = plain_rate_estimate(cg, p, (rows, 2 * rows))
+        out["speedup_vs_plain_fp64"] = value / out["plain_fp64"]["value_est"]
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def large_accuracy(cg, sub, n_slices):
+    """X and int_2e of the split form against the plain FP64 form on one r1 sample,
+    with int_2e compared in row blocks (one copy of it lives on the host)."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    nA2 = sub.n_ao ** 2
+    ns = sub.n_grid1
+    dr = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in sub.arrays().items()}
+
+    def build(prec, X, I):
+        opt = cg.options(prec, n_slices if prec == cg.SPLIT_BF16 else None, sub.a_en, sub.a_ee,
+                         3, True, 0, None)
+        s = cg.cutc_int_ex(opt, ns, sub.n_grid2, sub.n_ao, sub.n_nuc, sub.size_bh,
+                           dr["r1"], dr["wr1"], dr["r2"], dr["wr2"], dr["rn"], dr["aos1"],
+                           dr["aos2"], dr["c_bh"], dr["m_bh"], dr["n_bh"], dr["o_bh"], X, I, None)
+        torch.cuda.synchronize(dev)
+        if s != cg.CUTC_OK:
+            raise cg.CutcError(s, cg.last_error())
+
+    X = torch.empty((3, ns, nA2), dtype=torch.float64, device=dev)
+    I = torch.empty((nA2, nA2), dtype=torch.float64, device=dev)
+    build(cg.SPLIT_BF16, X, I)
+    Xs = X.cpu().numpy()
+    Is = I.cpu().numpy()
+    cg.load().cutc_release()
+    build(cg.PLAIN_FP64, X, I)
+    from oracle.oracle import rel_err
+    ex = rel_err(Xs, X.cpu().numpy())
+    d2 = r2 = 0.0
+    dmax = rmax = 0.0
+    step = max(1, (1 << 30) // (8 * nA2))
+    for r0 in range(0, nA2, step):
+        ref = I[r0:r0 + step].cpu().numpy()
+        d = Is[r0:r0 + step] - ref
+        d2 += float(np.sum(d * d))
+        r2 += float(np.sum(ref * ref))
+        dmax = max(dmax, float(np.max(np.abs(d))))
+        rmax = max(rmax, float(np.max(np.abs(ref))))
+    del X, I, dr
+    torch.cuda.empty_cache()
+    cg.load().cutc_release()
+    return {"X_vs_fp64": ex, "int2e_vs_fp64": {"norm": (d2 / r2) ** 0.5 if r2 > 0 else d2 ** 0.5,
+                                               "max": dmax / rmax if rmax > 0 else dmax}}
 
 
 def serving_requests(n, max_ao, seed=4004):
@@ -542,6 +759,8 @@ def main(argv=None):
     ap.add_argument("--scan", action="store_true", help="run the Jastrow-parameter scan instead")
     ap.add_argument("--sets", type=int, default=64)
     ap.add_argument("--scan-batch", type=int, default=8)
+    ap.add_argument("--r1-sample", type=int, default=6000,
+                    help="large workload: r1 rows of the bigger of the two timed samples")
     args = ap.parse_args(argv)
     if args.serving:
         return run_serving(args)
@@ -549,6 +768,8 @@ def main(argv=None):
         return run_scan(args)
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "large":
+        return run_large(args)
     return run_ours(args)
 
 
