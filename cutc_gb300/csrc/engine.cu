@@ -23,6 +23,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -93,6 +94,74 @@ int Workspace::get(int slot, size_t bytes, void **out)
     return CUTC_OK;
 }
 
+int PinnedPool::get(int k, size_t bytes, void **out)
+{
+    Buf &b = bufs[k];
+    bytes = std::max<size_t>(4096, (bytes + 4095) & ~(size_t)4095);
+    if (b.cap < bytes) {
+        if (b.p) {
+            cudaFreeHost(b.p);
+            b.p = nullptr;
+            b.cap = 0;
+        }
+        cudaError_t e = cudaHostAlloc(&b.p, bytes, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            b.p = nullptr;
+            cutc_set_error(CUTC_ERR_NO_MEMORY, "cudaHostAlloc(%zu) for output staging: %s", bytes,
+                           cudaGetErrorString(e));
+            return CUTC_ERR_NO_MEMORY;
+        }
+        b.cap = bytes;
+    }
+    *out = b.p;
+    return CUTC_OK;
+}
+
+void PinnedPool::release()
+{
+    for (auto &b : bufs) {
+        if (b.p)
+            cudaFreeHost(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+    }
+}
+
+// Host copy split over a few threads (page faults of fresh caller memory and
+// the copy itself both scale with threads).
+static void host_copy(void *dst, const void *src, size_t bytes)
+{
+    const size_t kChunk = (size_t)16 << 20;
+    const int n = (int)std::min<size_t>(4, bytes / kChunk);
+    if (n <= 1) {
+        memcpy(dst, src, bytes);
+        return;
+    }
+    const size_t per = ((bytes + n - 1) / n + 4095) & ~(size_t)4095;
+    std::vector<std::thread> th;
+    for (int k = 1; k < n; k++) {
+        const size_t o = (size_t)k * per;
+        if (o >= bytes)
+            break;
+        th.emplace_back([=] { memcpy((char *)dst + o, (const char *)src + o, std::min(per, bytes - o)); });
+    }
+    memcpy(dst, src, std::min(per, bytes));
+    for (auto &t : th)
+        t.join();
+}
+
+// True when the device can copy into p asynchronously (pinned, registered or managed).
+static bool async_host_ptr(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged;
+}
+
 void Workspace::release()
 {
     for (auto &b : bufs)
@@ -146,7 +215,9 @@ void destroy_engine(Engine *E)
     if (!E)
         return;
     cudaStreamSynchronize(E->stream);
+    cudaStreamSynchronize(E->xfer);
     E->ws.release();
+    E->pinned.release();
     for (auto e : E->tile_ev)
         cudaEventDestroy(e);
     for (int k = 0; k < kNumEvents; k++)
@@ -515,22 +586,61 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[2], st));
 
     // ---- tiles ---------------------------------------------------------------
-    // Host outputs leave through two staging buffers on the transfer stream; the
-    // copy of a tile is issued after the next tile is queued, so a copy into
-    // pageable memory (which holds the calling thread) overlaps device work.
+    // Host outputs leave through two device staging buffers, copied on the
+    // transfer stream while the next tile computes.  Pinned (or managed) caller
+    // memory takes the copies directly; pageable caller memory gets them in two
+    // pinned buffers first, from which this thread copies while the device
+    // works on (no pageable cudaMemcpy, which holds the thread until the stream
+    // reaches it).
     StreamsDrain drain{st, E->xfer};
     cudaEvent_t ready[2] = {E->ev[3], E->ev[4]}, done[2] = {E->ev[9], E->ev[10]};
     bool busy[2] = {false, false};
-    auto copy_x = [&](int tile) -> int {
+    const bool x_direct = out_dev || async_host_ptr(R.X);
+    const bool i_direct = out_dev || async_host_ptr(R.I);
+    double *hpin_x[2] = {nullptr, nullptr}, *hpin_i[2] = {nullptr, nullptr};
+    for (int k = 0; k < 2 && !out_dev; k++) {
+        if (!x_direct) {
+            CUTC_TRY(E->pinned.get(k, (size_t)R.x_components * n1t * nA2 * 8, &p));
+            hpin_x[k] = (double *)p;
+        }
+        if (!i_direct) {
+            CUTC_TRY(E->pinned.get(2 + k, (size_t)slab * nA2 * 8, &p));
+            hpin_i[k] = (double *)p;
+        }
+    }
+    auto tile_rows = [&](int tile, int64_t *i0, int64_t *nb) {
+        *i0 = (int64_t)tile * n1t;
+        *nb = std::min<int64_t>(n1t, n1 - *i0);
+    };
+    auto copy_x = [&](int tile) -> int {  // device staging -> caller memory or pinned
         const int b = tile & 1;
-        const int64_t i0 = (int64_t)tile * n1t, nb = std::min<int64_t>(n1t, n1 - i0);
+        int64_t i0, nb;
+        tile_rows(tile, &i0, &nb);
         CUTC_CUDA_TRY(cudaStreamWaitEvent(E->xfer, ready[b], 0));
-        for (int m = 0; m < R.x_components; m++)
-            CUTC_CUDA_TRY(cudaMemcpyAsync(R.X + ((int64_t)m * n1 + i0) * nA2,
-                                          stage_x[b] + (int64_t)m * nb * nA2,
-                                          (size_t)nb * nA2 * 8, cudaMemcpyDeviceToHost, E->xfer));
+        if (x_direct) {
+            for (int m = 0; m < R.x_components; m++)
+                CUTC_CUDA_TRY(cudaMemcpyAsync(R.X + ((int64_t)m * n1 + i0) * nA2,
+                                              stage_x[b] + (int64_t)m * nb * nA2,
+                                              (size_t)nb * nA2 * 8, cudaMemcpyDeviceToHost, E->xfer));
+        } else {
+            CUTC_CUDA_TRY(cudaMemcpyAsync(hpin_x[b], stage_x[b],
+                                          (size_t)R.x_components * nb * nA2 * 8,
+                                          cudaMemcpyDeviceToHost, E->xfer));
+        }
         CUTC_CUDA_TRY(cudaEventRecord(done[b], E->xfer));
         busy[b] = true;
+        return CUTC_OK;
+    };
+    auto finish_x = [&](int tile) -> int {  // pinned -> pageable caller memory
+        if (x_direct)
+            return CUTC_OK;
+        const int b = tile & 1;
+        int64_t i0, nb;
+        tile_rows(tile, &i0, &nb);
+        CUTC_CUDA_TRY(cudaEventSynchronize(done[b]));
+        for (int m = 0; m < R.x_components; m++)
+            host_copy(R.X + ((int64_t)m * n1 + i0) * nA2, hpin_x[b] + (int64_t)m * nb * nA2,
+                      (size_t)nb * nA2 * 8);
         return CUTC_OK;
     };
     CUBLAS_TRY(cublasSetStream(E->blas, st));
@@ -625,13 +735,14 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
                 CUTC_CUDA_TRY(cudaStreamWaitEvent(st, done[b], 0));
             CUTC_TRY(launch_expand_pairs(st, (int64_t)R.x_components * nb, nA, d_Xt, np, stage_x[b]));
             CUTC_CUDA_TRY(cudaEventRecord(ready[b], st));
+            CUTC_TRY(copy_x(tile));
             if (tile > 0)
-                CUTC_TRY(copy_x(tile - 1));
+                CUTC_TRY(finish_x(tile - 1));
         }
         note_launches(out_dev ? R.x_components : 1);
     }
     if (!out_dev && n_tiles > 0)
-        CUTC_TRY(copy_x(n_tiles - 1));
+        CUTC_TRY(finish_x(n_tiles - 1));
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[5], st));
 
     // ---- int_2e = A + A^T ------------------------------------------------------
@@ -639,17 +750,33 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, 0, (int)nA2, R.I));
         note_launches(1);
     } else {
-        // column slabs: assemble slab s while slab s - 1 is copied out
+        // column slabs: slab s is assembled while slab s - 1 is copied out
         const int n_slabs = (int)((nA2 + slab - 1) / slab);
         bool ibusy[2] = {false, false};
+        auto slab_cols = [&](int slab_no, int64_t *c0, int64_t *c1) {
+            *c0 = (int64_t)slab_no * slab;
+            *c1 = std::min<int64_t>(nA2, *c0 + slab);
+        };
         auto copy_i = [&](int slab_no) -> int {
             const int b = slab_no & 1;
-            const int64_t c0 = (int64_t)slab_no * slab, c1 = std::min<int64_t>(nA2, c0 + slab);
+            int64_t c0, c1;
+            slab_cols(slab_no, &c0, &c1);
             CUTC_CUDA_TRY(cudaStreamWaitEvent(E->xfer, ready[b], 0));
-            CUTC_CUDA_TRY(cudaMemcpyAsync(R.I + c0 * nA2, stage_i[b], (size_t)(c1 - c0) * nA2 * 8,
-                                          cudaMemcpyDeviceToHost, E->xfer));
+            CUTC_CUDA_TRY(cudaMemcpyAsync(i_direct ? R.I + c0 * nA2 : hpin_i[b], stage_i[b],
+                                          (size_t)(c1 - c0) * nA2 * 8, cudaMemcpyDeviceToHost,
+                                          E->xfer));
             CUTC_CUDA_TRY(cudaEventRecord(done[b], E->xfer));
             ibusy[b] = true;
+            return CUTC_OK;
+        };
+        auto finish_i = [&](int slab_no) -> int {
+            if (i_direct)
+                return CUTC_OK;
+            const int b = slab_no & 1;
+            int64_t c0, c1;
+            slab_cols(slab_no, &c0, &c1);
+            CUTC_CUDA_TRY(cudaEventSynchronize(done[b]));
+            host_copy(R.I + c0 * nA2, hpin_i[b], (size_t)(c1 - c0) * nA2 * 8);
             return CUTC_OK;
         };
         // the X copies still pending on the staging events must be waited for
@@ -659,16 +786,18 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
                 CUTC_CUDA_TRY(cudaStreamWaitEvent(st, done[b], 0));
         for (int sl = 0; sl < n_slabs; sl++) {
             const int b = sl & 1;
-            const int c0 = sl * slab, c1 = (int)std::min<int64_t>(nA2, (int64_t)c0 + slab);
+            int64_t c0, c1;
+            slab_cols(sl, &c0, &c1);
             if (ibusy[b])
                 CUTC_CUDA_TRY(cudaStreamWaitEvent(st, done[b], 0));
-            CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, c0, c1, stage_i[b]));
+            CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, (int)c0, (int)c1, stage_i[b]));
             note_launches(1);
             CUTC_CUDA_TRY(cudaEventRecord(ready[b], st));
+            CUTC_TRY(copy_i(sl));
             if (sl > 0)
-                CUTC_TRY(copy_i(sl - 1));
+                CUTC_TRY(finish_i(sl - 1));
         }
-        CUTC_TRY(copy_i(n_slabs - 1));
+        CUTC_TRY(finish_i(n_slabs - 1));
     }
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[7], st));
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[11], E->xfer));
@@ -963,5 +1092,7 @@ extern "C" void cutc_release(void)
         return;
     std::lock_guard<std::mutex> lk(E->mu);
     cudaStreamSynchronize(E->stream);
+    cudaStreamSynchronize(E->xfer);
     E->ws.release();
+    E->pinned.release();
 }

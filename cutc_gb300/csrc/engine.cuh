@@ -13,6 +13,18 @@ namespace cutc {
 
 constexpr int kNumEvents = 12;
 
+// Grow-only pinned host buffers: outputs bound for pageable caller memory leave
+// the device through them.
+struct PinnedPool {
+    struct Buf {
+        void *p = nullptr;
+        size_t cap = 0;
+    };
+    Buf bufs[4];
+    int get(int k, size_t bytes, void **out);
+    void release();
+};
+
 // Grow-only device buffers, one per slot, reused across calls.
 struct Workspace {
     struct Buf {
@@ -35,6 +47,7 @@ struct Engine {
     cudaEvent_t ev[kNumEvents];
     std::vector<cudaEvent_t> tile_ev;  // per-tile timing events (grown on demand)
     Workspace ws;
+    PinnedPool pinned;
     // Molecule-dependent operands left in the workspace by the previous build:
     // (molecule tag, buffer address) of the X-build A operand and of the int_2e
     // B operands.  A build with the same non-zero tag and the same buffer skips
