@@ -207,12 +207,14 @@ def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
 
 
 def scan_integrals(p, c_sets, a_en=None, a_ee=None, precision=PLAIN_FP64, n_slices=None,
-                   x_components=3, with_stats=False):
+                   x_components=3, with_stats=False, out=None):
     """Jastrow-parameter scan on one molecule (cutc_int_scan).
 
     c_sets: (n_sets, n_nuc, size_bh) coefficients (the exponents of p are used for
     every set); a_en / a_ee: per-set scale factors or None.  Returns
-    X (n_sets, x_components, n1, nA^2) and int_2e (n_sets, nA^2, nA^2).
+    X (n_sets, x_components, n1, nA^2) and int_2e (n_sets, nA^2, nA^2); out=(X, I)
+    gives C-contiguous float64 arrays of those shapes (pinned memory is copied
+    into directly) to fill instead of new ones.
     """
     c_sets = np.ascontiguousarray(c_sets, dtype=np.float64)
     ns = c_sets.shape[0]
@@ -220,8 +222,14 @@ def scan_integrals(p, c_sets, a_en=None, a_ee=None, precision=PLAIN_FP64, n_slic
     m, n, o = rep(p.m_bh), rep(p.n_bh), rep(p.o_bh)
     ae = None if a_en is None else np.ascontiguousarray(a_en, dtype=np.float64)
     aee = None if a_ee is None else np.ascontiguousarray(a_ee, dtype=np.float64)
-    X = np.empty((ns, x_components, p.n_grid1, p.n_ao ** 2))
-    I = np.empty((ns, p.n_ao ** 2, p.n_ao ** 2))
+    if out is None:
+        X = np.empty((ns, x_components, p.n_grid1, p.n_ao ** 2))
+        I = np.empty((ns, p.n_ao ** 2, p.n_ao ** 2))
+    else:
+        X, I = out
+        assert X.shape == (ns, x_components, p.n_grid1, p.n_ao ** 2) and X.dtype == np.float64
+        assert I.shape == (ns, p.n_ao ** 2, p.n_ao ** 2) and I.dtype == np.float64
+        assert X.flags.c_contiguous and I.flags.c_contiguous
     opt = options(precision, n_slices, p.a_en, p.a_ee, x_components)
     st = Stats()
     arrs = [p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2, c_sets, m, n, o]

@@ -560,8 +560,10 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     SplitPlan sp;
     float2 *d_r2d = nullptr, *d_f2d = nullptr, *d_poly = nullptr;
     int pexp = 4;
+    bool psparse = false;
     if (R.precision == CUTC_SPLIT_BF16) {
         pexp = pair_df_max_exp(exps.data(), nt);
+        psparse = pexp == 4 && pair_df_sparse(exps.data(), nt) && !getenv("CUTC_PAIR_DENSE");
         CUTC_TRY(W.get(S_R2D, 3 * (size_t)n2 * sizeof(float2), &p));
         d_r2d = (float2 *)p;
         CUTC_TRY(W.get(S_F2D, (size_t)nN * n2 * sizeof(float2), &p));
@@ -675,7 +677,7 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
             P.a_ee_hi = (float)R.a_ee;
             P.a_ee_lo = (float)(R.a_ee - (double)P.a_ee_hi);
             P.G = reinterpret_cast<float2 *>(d_G); P.ldg = n2; P.plane = (int64_t)nb * n2;
-            CUTC_TRY(launch_pair_df(st, P, pexp, d_rn, R.a_en));
+            CUTC_TRY(launch_pair_df(st, P, pexp, psparse, d_rn, R.a_en));
             note_launches(3);
         }
         if (tev)

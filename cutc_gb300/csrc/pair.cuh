@@ -53,12 +53,15 @@ struct PairDfArgs {
 };
 
 int pair_df_max_exp(const int *exps, int n_terms);
+// True when every exponent of the term table is 0, 2, 3 or 4 (the sparse-power kernel applies).
+bool pair_df_sparse(const int *exps, int n_terms);
 // in place: x[i] (FP64) -> (hi, lo) float pair at the same 8 bytes
 int launch_f64_to_df(cudaStream_t st, double *x, int64_t n);
 size_t pair_df_poly_bytes(int E, int n1b, int nN);
 int launch_r2_df(cudaStream_t st, int n2, int nN, const double *r2, const double *f2, float2 *r2d,
                  float2 *f2d);
-int launch_pair_df(cudaStream_t st, const PairDfArgs &P, int E, const double *rn, double a_en);
+int launch_pair_df(cudaStream_t st, const PairDfArgs &P, int E, bool sparse, const double *rn,
+                   double a_en);
 
 int launch_r1_terms(cudaStream_t st, int i0, int n, int nN, const double *r1, const double *rn,
                     double a, NucTerm *t1);

@@ -81,3 +81,18 @@ def test_drop_in_env_selects_split(monkeypatch):
                     p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I)
     assert s == 0, cg.last_error()
     _check(X, I, ref["X"], ref["int2e"])
+
+
+def test_sparse_power_pair_kernel_matches_general(monkeypatch):
+    """Exponents in {0, 2, 3, 4} select the sparse-power df pair kernel; the general
+    kernel (CUTC_PAIR_DENSE) evaluates the same polynomials in another order."""
+    p = synth.make_problem(n_nuc=4, n_ao=9, n_grid1=300, n_grid2=1200, size_bh=9, seed=17,
+                           a_en=0.8, a_ee=1.3)
+    assert set(np.unique(np.concatenate([p.m_bh.ravel(), p.n_bh.ravel(), p.o_bh.ravel()]))) <= {0, 2, 3, 4}
+    X1, I1 = cg.build_integrals(p, cg.SPLIT_BF16, x_components=4)
+    monkeypatch.setenv("CUTC_PAIR_DENSE", "1")
+    X2, I2 = cg.build_integrals(p, cg.SPLIT_BF16, x_components=4)
+    assert oracle.rel_err(X1, X2)["max"] < 1e-12
+    assert oracle.rel_err(I1, I2)["max"] < 1e-12
+    Xo, Io = oracle.cutc_int(p)
+    _check(X1[:3], I1, Xo, Io)
