@@ -249,14 +249,25 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const int q = warp & 3, cgrp = warp >> 2;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         const uint32_t coff = (uint32_t)(CW * cgrp);
-        float hi0[CW], lo0[CW], hi1[CW], lo1[CW], hi2[CW], lo2[CW], s3[CW];
+        // column pairs packed in 64 bits: every add below is one f32x2 instruction for
+        // two columns (round to nearest in each lane, as the scalar form)
+        constexpr int CP = CW / 2;
+        uint64_t hi0[CP], lo0[CP], hi1[CP], lo1[CP], hi2[CP], lo2[CP], s3[CP];
 #pragma unroll
-        for (int j = 0; j < CW; j++)
-            hi0[j] = lo0[j] = hi1[j] = lo1[j] = hi2[j] = lo2[j] = s3[j] = 0.f;
+        for (int j = 0; j < CP; j++)
+            hi0[j] = lo0[j] = hi1[j] = lo1[j] = hi2[j] = lo2[j] = s3[j] = 0ull;
         // v + C - C rounds v to the grid of C's binade: C = 1.5 2^(23 + g) gives multiples of 2^g
-        const float C0 = 786432.0f;  // 1.5 * 2^19: multiples of 2^-4  (d = 0, LSB 2^-16)
-        const float C1 = 1536.0f;    // 1.5 * 2^10: multiples of 2^-13 (d = 1, LSB 2^-25)
-        const float C2 = 3.0f;       // 1.5 * 2^1:  multiples of 2^-22 (d = 2, LSB 2^-34)
+        const uint64_t C0 = tc::f2_pack(__float_as_uint(786432.0f), __float_as_uint(786432.0f));
+        // 1.5 * 2^19: multiples of 2^-4  (d = 0, LSB 2^-16)
+        const uint64_t C1 = tc::f2_pack(__float_as_uint(1536.0f), __float_as_uint(1536.0f));
+        // 1.5 * 2^10: multiples of 2^-13 (d = 1, LSB 2^-25)
+        const uint64_t C2 = tc::f2_pack(__float_as_uint(3.0f), __float_as_uint(3.0f));
+        // 1.5 * 2^1:  multiples of 2^-22 (d = 2, LSB 2^-34)
+        auto exact_add = [](uint64_t x, uint64_t Cg, uint64_t &hi, uint64_t &lo) {
+            const uint64_t hh = tc::f2_sub(tc::f2_add(x, Cg), Cg);
+            hi = tc::f2_add(hi, hh);
+            lo = tc::f2_add(lo, tc::f2_sub(x, hh));
+        };
         bool ok = true;
         for (int c = 0; c < nch; c++) {
             const int b = c & 1;
@@ -269,39 +280,27 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 #pragma unroll
             for (int h = 0; h < CW / 4; h++) {
                 const uint32_t cb = tbase + lane_off + (uint32_t)(Cfg::kBuf * b) + coff + 4u * h;
-                float v[4];
-                tc::tmem_ld4(cb, v);
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const float x = v[j];
-                    const float hh = __fsub_rn(__fadd_rn(x, C0), C0);
-                    hi0[4 * h + j] = __fadd_rn(hi0[4 * h + j], hh);
-                    lo0[4 * h + j] = __fadd_rn(lo0[4 * h + j], __fsub_rn(x, hh));
-                }
-                tc::tmem_ld4(cb + BN, v);
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const float x = v[j];
-                    const float hh = __fsub_rn(__fadd_rn(x, C1), C1);
-                    hi1[4 * h + j] = __fadd_rn(hi1[4 * h + j], hh);
-                    lo1[4 * h + j] = __fadd_rn(lo1[4 * h + j], __fsub_rn(x, hh));
-                }
+                uint32_t v[4];
+                tc::tmem_ld4_nowait(cb, v);
+                tc::tmem_wait_ld();
+                exact_add(tc::f2_pack(v[0], v[1]), C0, hi0[2 * h], lo0[2 * h]);
+                exact_add(tc::f2_pack(v[2], v[3]), C0, hi0[2 * h + 1], lo0[2 * h + 1]);
+                tc::tmem_ld4_nowait(cb + BN, v);
+                tc::tmem_wait_ld();
+                exact_add(tc::f2_pack(v[0], v[1]), C1, hi1[2 * h], lo1[2 * h]);
+                exact_add(tc::f2_pack(v[2], v[3]), C1, hi1[2 * h + 1], lo1[2 * h + 1]);
                 if (D >= 2) {
-                    tc::tmem_ld4(cb + 2 * BN, v);
-#pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        const float x = v[j];
-                        const float hh = __fsub_rn(__fadd_rn(x, C2), C2);
-                        hi2[4 * h + j] = __fadd_rn(hi2[4 * h + j], hh);
-                        lo2[4 * h + j] = __fadd_rn(lo2[4 * h + j], __fsub_rn(x, hh));
-                    }
+                    tc::tmem_ld4_nowait(cb + 2 * BN, v);
+                    tc::tmem_wait_ld();
+                    exact_add(tc::f2_pack(v[0], v[1]), C2, hi2[2 * h], lo2[2 * h]);
+                    exact_add(tc::f2_pack(v[2], v[3]), C2, hi2[2 * h + 1], lo2[2 * h + 1]);
                 }
 #pragma unroll
                 for (int d = 3; d <= D; d++) {
-                    tc::tmem_ld4(cb + d * BN, v);
-#pragma unroll
-                    for (int j = 0; j < 4; j++)
-                        s3[4 * h + j] = __fadd_rn(s3[4 * h + j], v[j]);
+                    tc::tmem_ld4_nowait(cb + d * BN, v);
+                    tc::tmem_wait_ld();
+                    s3[2 * h] = tc::f2_add(s3[2 * h], tc::f2_pack(v[0], v[1]));
+                    s3[2 * h + 1] = tc::f2_add(s3[2 * h + 1], tc::f2_pack(v[2], v[3]));
                 }
             }
             tc::fence_before_sync();
@@ -316,9 +315,11 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             for (int j = 0; j < CW; j++) {
                 const int n = n0 + (int)coff + j;
                 if (n < P.N) {
-                    double val = (((double)hi0[j] + (double)hi1[j]) +
-                                  ((double)hi2[j] + (double)lo0[j])) +
-                                 (((double)lo1[j] + (double)lo2[j]) + (double)s3[j]);
+                    auto lane_of = [&](const uint64_t (&a)[CP]) -> double {
+                        return (double)((j & 1) ? tc::f2_hi(a[j >> 1]) : tc::f2_lo(a[j >> 1]));
+                    };
+                    double val = ((lane_of(hi0) + lane_of(hi1)) + (lane_of(hi2) + lane_of(lo0))) +
+                                 ((lane_of(lo1) + lane_of(lo2)) + lane_of(s3));
                     val *= P.alpha * pow2(em + P.eb[n]);
                     const int64_t col = (int64_t)(n / P.ncol_group) * P.group_stride + P.col0 +
                                         n % P.ncol_group;

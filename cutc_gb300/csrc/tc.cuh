@@ -215,6 +215,30 @@ __device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8])
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
+// Two FP32 lanes packed in 64 bits (x in the low word): round-to-nearest
+// add / sub of both lanes in one instruction (sm_100 and later).
+__device__ __forceinline__ uint64_t f2_pack(uint32_t lo, uint32_t hi)
+{
+    return ((uint64_t)hi << 32) | lo;
+}
+
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b)
+{
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b)
+{
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+__device__ __forceinline__ float f2_lo(uint64_t a) { return __uint_as_float((uint32_t)a); }
+__device__ __forceinline__ float f2_hi(uint64_t a) { return __uint_as_float((uint32_t)(a >> 32)); }
+
 // Shared-memory matrix descriptor (tcgen05), K-major operand with 64-byte
 // swizzling: rows of 64 B, 8-row groups 512 B apart (stride byte offset).
 __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr)
