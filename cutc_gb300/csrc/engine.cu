@@ -341,7 +341,7 @@ static int validate(const Request &R)
 enum Slot {
     S_R1, S_WR1, S_R2, S_WR2, S_RN, S_AOS1, S_AOS2, S_COEF, S_EXPS, S_OFF,
     S_T1, S_F2, S_P, S_G, S_XP, S_S0, S_SL, S_H, S_N, S_XOUT, S_XOUT1, S_IOUT, S_IOUT1,
-    S_R2D, S_F2D, S_POLY,
+    S_R2D, S_F2D, S_POLY, S_BLASWS,
     S_SPLIT0  // split-form slots follow
 };
 
@@ -645,7 +645,13 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
                       (size_t)nb * nA2 * 8);
         return CUTC_OK;
     };
+    // cuBLAS gets its workspace from the engine (no allocation inside a build)
     CUBLAS_TRY(cublasSetStream(E->blas, st));
+    if (R.precision == CUTC_PLAIN_FP64) {
+        const size_t blas_ws = (size_t)32 << 20;
+        CUTC_TRY(W.get(S_BLASWS, blas_ws, &p));
+        CUBLAS_TRY(cublasSetWorkspace(E->blas, p, blas_ws));
+    }
     for (int tile = 0; tile < n_tiles; tile++) {
         const int i0 = (int)(tile * n1t);
         const int nb = (int)std::min<int64_t>(n1t, n1 - i0);
