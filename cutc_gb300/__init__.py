@@ -32,7 +32,11 @@ SPLIT_BF16 = 1
 EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_int_scan", "cutc_default_options", "cutc_jast_bh_dev",
            "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_validate_launch_dims",
            "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
-           "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy"]
+           "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy",
+           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy"]
+
+INT2E_PQST = 0
+INT2E_PSQT = 1
 
 
 class Options(ctypes.Structure):
@@ -40,7 +44,8 @@ class Options(ctypes.Structure):
                 ("a_en", ctypes.c_double), ("a_ee", ctypes.c_double),
                 ("x_components", ctypes.c_int), ("device_pointers", ctypes.c_int),
                 ("max_work_bytes", ctypes.c_size_t), ("stream", ctypes.c_void_p),
-                ("pair_fp64", ctypes.c_int), ("k_split", ctypes.c_int)]
+                ("pair_fp64", ctypes.c_int), ("k_split", ctypes.c_int),
+                ("int2e_layout", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -120,6 +125,12 @@ def load(path: str = LIB_PATH):
     L.cutc_last_error.restype = ctypes.c_char_p
     L.cutc_release.argtypes = []
     L.cutc_release.restype = None
+    L.trans_inplace.argtypes = [vp, i]
+    L.trans_inplace.restype = None
+    L.trans_pqst_psqt_inplace.argtypes = [i, vp]
+    L.trans_pqst_psqt_inplace.restype = None
+    L.trans_pqst_psqt_copy.argtypes = [i, vp, vp]
+    L.trans_pqst_psqt_copy.restype = None
     L.cutc_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
     L.cutc_server_default_config.restype = None
     L.cutc_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
@@ -161,7 +172,7 @@ def cutc_int(nxBlocks, nyBlocks, nzBlocks, blockxSize, blockySize, blockzSize,
 
 def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_components=3,
             device_pointers=False, max_work_bytes=0, stream=None, pair_fp64=False,
-            k_split=0) -> Options:
+            k_split=0, int2e_layout=INT2E_PQST) -> Options:
     o = Options()
     load().cutc_default_options(ctypes.byref(o))
     o.precision = precision
@@ -174,6 +185,7 @@ def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_component
     o.stream = stream
     o.pair_fp64 = 1 if pair_fp64 else 0
     o.k_split = k_split
+    o.int2e_layout = int2e_layout
     return o
 
 
@@ -187,7 +199,8 @@ def cutc_int_ex(opt: Options, n_grid1, n_grid2, n_ao, n_nuc, size_bh,
 
 
 def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
-                    max_work_bytes=0, with_stats=False, pair_fp64=False, k_split=0):
+                    max_work_bytes=0, with_stats=False, pair_fp64=False, k_split=0,
+                    int2e_layout=INT2E_PQST):
     """Host-array convenience call on a synth.Problem: returns (X, int_2e[, stats]).
 
     X is (x_components, n1, nA^2) == Fortran (nA, nA, n1, comps); int_2e is
@@ -197,7 +210,7 @@ def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
     I = np.empty((p.n_ao ** 2, p.n_ao ** 2))
     st = Stats()
     opt = options(precision, n_slices, p.a_en, p.a_ee, x_components, False, max_work_bytes,
-                  None, pair_fp64, k_split)
+                  None, pair_fp64, k_split, int2e_layout)
     s = cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
                     p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2,
                     p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I, st)

@@ -323,6 +323,10 @@ static int validate(const Request &R)
         cutc_set_error(CUTC_ERR_INVALID, "unknown precision form %d", R.precision);
         return CUTC_ERR_INVALID;
     }
+    if (R.int2e_layout != CUTC_INT2E_PQST && R.int2e_layout != CUTC_INT2E_PSQT) {
+        cutc_set_error(CUTC_ERR_INVALID, "unknown int_2e layout %d", R.int2e_layout);
+        return CUTC_ERR_INVALID;
+    }
     if (R.k_split < 0 || (R.k_split > 0 && R.k_split < 64)) {
         cutc_set_error(CUTC_ERR_INVALID, "k_split must be 0 or at least 64");
         return CUTC_ERR_INVALID;
@@ -353,15 +357,18 @@ static inline double ev_ms(cudaEvent_t a, cudaEvent_t b)
 }
 
 // Columns of int_2e per output slab when int_2e goes to the host: a slab is
-// assembled on the device and copied out while the next one is assembled.
-// CUTC_INT2E_SLAB_COLS overrides the 1 GiB slab (rounded down to 32 columns).
+// assembled on the device and copied out while the next one is assembled.  A
+// slab is a whole number of the slowest index t (nA columns), so it is one
+// contiguous block in both int_2e layouts.
+// CUTC_INT2E_SLAB_COLS overrides the 1 GiB slab (rounded down to nA columns).
 static int int2e_slab_cols(int nA)
 {
     const int64_t n = (int64_t)nA * nA;
-    int64_t per = (((int64_t)1 << 30) / (n * 8)) / 32 * 32;
+    int64_t per = ((int64_t)1 << 30) / (n * 8);
     if (const char *e = getenv("CUTC_INT2E_SLAB_COLS"))
-        per = atoll(e) / 32 * 32;
-    return (int)std::min<int64_t>(n, std::max<int64_t>(32, per));
+        per = atoll(e);
+    per = per / nA * nA;
+    return (int)std::min<int64_t>(n, std::max<int64_t>(nA, per));
 }
 
 // Device bytes of a build that do not grow with the r1 tile (besides the
@@ -754,8 +761,9 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[5], st));
 
     // ---- int_2e = A + A^T ------------------------------------------------------
+    const bool psqt = R.int2e_layout == CUTC_INT2E_PSQT;
     if (out_dev) {
-        CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, 0, (int)nA2, R.I));
+        CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, 0, (int)nA2, psqt, R.I));
         note_launches(1);
     } else {
         // column slabs: slab s is assembled while slab s - 1 is copied out
@@ -798,7 +806,7 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
             slab_cols(sl, &c0, &c1);
             if (ibusy[b])
                 CUTC_CUDA_TRY(cudaStreamWaitEvent(st, done[b], 0));
-            CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, (int)c0, (int)c1, stage_i[b]));
+            CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, (int)c0, (int)c1, psqt, stage_i[b]));
             note_launches(1);
             CUTC_CUDA_TRY(cudaEventRecord(ready[b], st));
             CUTC_TRY(copy_i(sl));
@@ -936,6 +944,7 @@ extern "C" int cutc_int_ex(const cutc_options *opt, int n_grid1, int n_grid2, in
     R.stream = (cudaStream_t)opt->stream;
     R.pair_fp64 = opt->pair_fp64;
     R.k_split = opt->k_split;
+    R.int2e_layout = opt->int2e_layout;
     R.n1 = n_grid1; R.n2 = n_grid2; R.nA = n_ao; R.nN = n_nuc; R.nB = size_bh;
     R.r1 = r1; R.wr1 = wr1; R.r2 = r2; R.wr2 = wr2; R.rn = rn;
     R.aos1 = aos_data1; R.aos2 = aos_data2;
@@ -984,6 +993,7 @@ extern "C" int cutc_int_scan(const cutc_options *opt, int n_sets, int n_grid1, i
     base.stream = (cudaStream_t)opt->stream;
     base.pair_fp64 = opt->pair_fp64;
     base.k_split = opt->k_split;
+    base.int2e_layout = opt->int2e_layout;
     base.n1 = n_grid1; base.n2 = n_grid2; base.nA = n_ao; base.nN = n_nuc; base.nB = size_bh;
     base.r1 = r1; base.wr1 = wr1; base.r2 = r2; base.wr2 = wr2; base.rn = rn;
     base.aos1 = aos_data1; base.aos2 = aos_data2;

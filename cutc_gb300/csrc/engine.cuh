@@ -70,6 +70,7 @@ struct Request {
     int tile_rows = 0;  // optional cap on r1 rows per tile
     int pair_fp64 = 0;  // split form: FP64 pair terms
     int k_split = 0;    // split form: max K per tensor-core launch (0 = default)
+    int int2e_layout = CUTC_INT2E_PQST;
     uint64_t mol_tag = 0;  // non-zero: molecule arrays identical to earlier builds with this tag
     cudaStream_t stream = nullptr;
     int n1 = 0, n2 = 0, nA = 0, nN = 0, nB = 0;

@@ -94,7 +94,9 @@ __device__ __forceinline__ double a_entry(int row, int col, int nA, int64_t np,
 }
 
 // out[row + n (col - c0)] = A[row, col] + A[col, row] for the columns
-// c0 <= col < c1, n = nA^2, 32x32 tiles
+// c0 <= col < c1, n = nA^2, 32x32 tiles.  PSQT: row = p + nA q, col = s + nA t
+// goes to p + nA s + nA^2 q + nA^3 (t - c0 / nA) instead.
+template <bool PSQT>
 __global__ void assemble_int2e_kernel(int nA, const double *__restrict__ H,
                                       const double *__restrict__ N, int c0, int c1,
                                       double *__restrict__ out)
@@ -118,8 +120,16 @@ __global__ void assemble_int2e_kernel(int nA, const double *__restrict__ H,
     for (int k = 0; k < 4; k++) {
         const int row = R0 + tx, col = C0 + ty + 8 * k;
         // t[i][j] = A[C0 + j, R0 + i]  ->  A[col, row] = t[tx][ty + 8k]
-        if (row < n && col < c1)
-            out[row + (int64_t)n * (col - c0)] = v[k] + t[tx][ty + 8 * k];
+        if (row < n && col < c1) {
+            int64_t o;
+            if (PSQT) {
+                const int p = row % nA, q = row / nA, s_ = col % nA, tt = col / nA - c0 / nA;
+                o = p + (int64_t)nA * s_ + (int64_t)n * q + (int64_t)n * nA * tt;
+            } else {
+                o = row + (int64_t)n * (col - c0);
+            }
+            out[o] = v[k] + t[tx][ty + 8 * k];
+        }
     }
 }
 
@@ -162,13 +172,20 @@ int launch_expand_pairs(cudaStream_t st, int64_t rows, int nA, const double *Xp,
 }
 
 int launch_assemble_int2e(cudaStream_t st, int nA, const double *H, const double *N, int c0,
-                          int c1, double *out)
+                          int c1, bool psqt, double *out)
 {
     const int n = nA * nA;
     if (c0 < 0 || c1 > n || c0 >= c1)
         return CUTC_OK;
+    if (psqt && (c0 % nA || c1 % nA)) {
+        cutc_set_error(CUTC_ERR_INVALID, "int_2e slab [%d, %d) is not a whole number of t", c0, c1);
+        return CUTC_ERR_INVALID;
+    }
     dim3 grid(ceil_div(n, 32), ceil_div(c1 - c0, 32));
-    assemble_int2e_kernel<<<grid, dim3(32, 8), 0, st>>>(nA, H, N, c0, c1, out);
+    if (psqt)
+        assemble_int2e_kernel<true><<<grid, dim3(32, 8), 0, st>>>(nA, H, N, c0, c1, out);
+    else
+        assemble_int2e_kernel<false><<<grid, dim3(32, 8), 0, st>>>(nA, H, N, c0, c1, out);
     CUTC_CUDA_TRY(cudaGetLastError());
     return CUTC_OK;
 }

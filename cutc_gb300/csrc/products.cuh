@@ -18,7 +18,8 @@ int launch_expand_pairs(cudaStream_t st, int64_t rows, int nA, const double *Xp,
                         double *X);
 // Columns c0 <= col < c1 of int_2e = A + A^T (column-major, nA^2 rows) from the
 // packed symmetric (H) and antisymmetric (N) parts; out holds column c0 first.
+// psqt: element (p,q,s,t) goes where (p,s,q,t) would (c0 and c1 multiples of nA).
 int launch_assemble_int2e(cudaStream_t st, int nA, const double *H, const double *N, int c0,
-                          int c1, double *out);
+                          int c1, bool psqt, double *out);
 
 }  // namespace cutc

@@ -228,6 +228,7 @@ static Request to_request(const cutc_request &q)
     R.x_components = o.x_components;
     R.pair_fp64 = o.pair_fp64;
     R.k_split = o.k_split;
+    R.int2e_layout = o.int2e_layout;
     R.n1 = q.n_grid1; R.n2 = q.n_grid2; R.nA = q.n_ao; R.nN = q.n_nuc; R.nB = q.size_bh;
     R.r1 = q.r1; R.wr1 = q.wr1; R.r2 = q.r2; R.wr2 = q.wr2; R.rn = q.rn;
     R.aos1 = q.aos_data1; R.aos2 = q.aos_data2;

@@ -68,7 +68,13 @@ typedef struct cutc_options {
     int pair_fp64;          /* split form: 1 = pair terms in FP64 instead of double-float */
     int k_split;            /* split form: max K per tensor-core launch; the partial results
                                are summed in FP64 (0 = 262144) */
+    int int2e_layout;       /* CUTC_INT2E_PQST (reference order) or CUTC_INT2E_PSQT: int_2e with
+                               its 2nd and 3rd indices swapped, as trans_pqst_psqt_inplace
+                               leaves it (the order cutc_no uses), written directly */
 } cutc_options;
+
+#define CUTC_INT2E_PQST 0
+#define CUTC_INT2E_PSQT 1
 
 typedef struct cutc_stats {
     double ms_total;        /* wall time of the call */
@@ -223,6 +229,21 @@ int cutc_server_wait(cutc_server *server, unsigned long long ticket, double *lat
 int cutc_server_get_stats(cutc_server *server, cutc_server_stats *stats);
 /* Finishes the queued requests, then frees the contexts and the cache. */
 void cutc_server_destroy(cutc_server *server);
+
+/* ---- reference helpers with the reference's names and semantics ------------
+ * Device pointers; launched on the legacy default stream without a host
+ * synchronisation, as the reference does; errors are recorded for
+ * cutc_last_error() (the reference signatures return nothing).
+ *
+ * trans_inplace (src/add_trans_inplace.cu:25-35): data <- data + data^T for a
+ * size x size column-major matrix.
+ * trans_pqst_psqt_inplace (src/trans_pqst_psqt_inplace.cu:50-62): the
+ * size^4 array data(p,q,s,t) (column-major) becomes data(p,s,q,t).
+ * trans_pqst_psqt_copy (src/trans_pqst_psqt_copy.cu:45-57): data_new(p,q,s,t)
+ * = data_old(p,s,q,t).  No reference counterpart besides those files. */
+void trans_inplace(double *data, int size);
+void trans_pqst_psqt_inplace(int size, double *data);
+void trans_pqst_psqt_copy(int size, double *data_old, double *data_new);
 
 /* Message describing the last non-zero status returned on this thread. */
 const char *cutc_last_error(void);

@@ -15,7 +15,7 @@ def declared_functions():
         if fn.endswith(".h"):
             text = open(os.path.join(ROOT, "include", fn)).read()
             text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-            names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(cutc_\w+)\s*\(", text, flags=re.M)
+            names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(\w+)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 
