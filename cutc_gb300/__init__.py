@@ -33,10 +33,28 @@ EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_int_scan", "cutc_default_options", "
            "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_validate_launch_dims",
            "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
            "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy",
-           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy"]
+           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos"]
 
 INT2E_PQST = 0
 INT2E_PSQT = 1
+
+
+class Basis(ctypes.Structure):
+    _fields_ = [("n_ao", ctypes.c_int), ("center", ctypes.c_void_p), ("power", ctypes.c_void_p),
+                ("prim_offset", ctypes.c_void_p), ("prim_exp", ctypes.c_void_p),
+                ("prim_coef", ctypes.c_void_p)]
+
+
+def make_basis(shells):
+    """A cutc_basis for synth shells; the returned object keeps its arrays alive."""
+    from .synth import basis_arrays
+    arrs = basis_arrays(shells)
+    b = Basis()
+    b.n_ao = arrs["center"].shape[0]
+    for k in ("center", "power", "prim_offset", "prim_exp", "prim_coef"):
+        setattr(b, k, arrs[k].ctypes.data)
+    b._arrays = arrs
+    return b
 
 
 class Options(ctypes.Structure):
@@ -45,7 +63,7 @@ class Options(ctypes.Structure):
                 ("x_components", ctypes.c_int), ("device_pointers", ctypes.c_int),
                 ("max_work_bytes", ctypes.c_size_t), ("stream", ctypes.c_void_p),
                 ("pair_fp64", ctypes.c_int), ("k_split", ctypes.c_int),
-                ("int2e_layout", ctypes.c_int)]
+                ("int2e_layout", ctypes.c_int), ("basis", ctypes.c_void_p)]
 
 
 class Stats(ctypes.Structure):
@@ -131,6 +149,8 @@ def load(path: str = LIB_PATH):
     L.trans_pqst_psqt_inplace.restype = None
     L.trans_pqst_psqt_copy.argtypes = [i, vp, vp]
     L.trans_pqst_psqt_copy.restype = None
+    L.cutc_eval_aos.argtypes = [ctypes.POINTER(Basis), i, vp, i, vp, i, vp]
+    L.cutc_eval_aos.restype = i
     L.cutc_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
     L.cutc_server_default_config.restype = None
     L.cutc_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
@@ -152,6 +172,8 @@ def last_error() -> str:
 
 
 def _vp(a):
+    if a is None:
+        return None
     if hasattr(a, "data_ptr"):
         return ctypes.c_void_p(a.data_ptr())
     assert a.flags.c_contiguous
@@ -172,7 +194,7 @@ def cutc_int(nxBlocks, nyBlocks, nzBlocks, blockxSize, blockySize, blockzSize,
 
 def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_components=3,
             device_pointers=False, max_work_bytes=0, stream=None, pair_fp64=False,
-            k_split=0, int2e_layout=INT2E_PQST) -> Options:
+            k_split=0, int2e_layout=INT2E_PQST, basis=None) -> Options:
     o = Options()
     load().cutc_default_options(ctypes.byref(o))
     o.precision = precision
@@ -186,6 +208,9 @@ def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_component
     o.pair_fp64 = 1 if pair_fp64 else 0
     o.k_split = k_split
     o.int2e_layout = int2e_layout
+    if basis is not None:
+        o.basis = ctypes.addressof(basis)
+        o._basis = basis  # keeps the basis alive with the options
     return o
 
 
@@ -200,7 +225,7 @@ def cutc_int_ex(opt: Options, n_grid1, n_grid2, n_ao, n_nuc, size_bh,
 
 def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
                     max_work_bytes=0, with_stats=False, pair_fp64=False, k_split=0,
-                    int2e_layout=INT2E_PQST):
+                    int2e_layout=INT2E_PQST, aos_from_basis=False):
     """Host-array convenience call on a synth.Problem: returns (X, int_2e[, stats]).
 
     X is (x_components, n1, nA^2) == Fortran (nA, nA, n1, comps); int_2e is
@@ -209,10 +234,12 @@ def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
     X = np.empty((x_components, p.n_grid1, p.n_ao ** 2))
     I = np.empty((p.n_ao ** 2, p.n_ao ** 2))
     st = Stats()
+    basis = make_basis(p.shells) if aos_from_basis else None
     opt = options(precision, n_slices, p.a_en, p.a_ee, x_components, False, max_work_bytes,
-                  None, pair_fp64, k_split, int2e_layout)
+                  None, pair_fp64, k_split, int2e_layout, basis)
+    aos1, aos2 = (None, None) if aos_from_basis else (p.aos1, p.aos2)
     s = cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
-                    p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2,
+                    p.r1, p.wr1, p.r2, p.wr2, p.rn, aos1, aos2,
                     p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I, st)
     if s != CUTC_OK:
         raise CutcError(s, last_error())
@@ -220,14 +247,15 @@ def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
 
 
 def scan_integrals(p, c_sets, a_en=None, a_ee=None, precision=PLAIN_FP64, n_slices=None,
-                   x_components=3, with_stats=False, out=None):
+                   x_components=3, with_stats=False, out=None, basis=None):
     """Jastrow-parameter scan on one molecule (cutc_int_scan).
 
     c_sets: (n_sets, n_nuc, size_bh) coefficients (the exponents of p are used for
     every set); a_en / a_ee: per-set scale factors or None.  Returns
     X (n_sets, x_components, n1, nA^2) and int_2e (n_sets, nA^2, nA^2); out=(X, I)
     gives C-contiguous float64 arrays of those shapes (pinned memory is copied
-    into directly) to fill instead of new ones.
+    into directly) to fill instead of new ones; basis (make_basis) replaces the AO
+    arrays, which are then evaluated on the GPU once for all sets.
     """
     c_sets = np.ascontiguousarray(c_sets, dtype=np.float64)
     ns = c_sets.shape[0]
@@ -243,9 +271,10 @@ def scan_integrals(p, c_sets, a_en=None, a_ee=None, precision=PLAIN_FP64, n_slic
         assert X.shape == (ns, x_components, p.n_grid1, p.n_ao ** 2) and X.dtype == np.float64
         assert I.shape == (ns, p.n_ao ** 2, p.n_ao ** 2) and I.dtype == np.float64
         assert X.flags.c_contiguous and I.flags.c_contiguous
-    opt = options(precision, n_slices, p.a_en, p.a_ee, x_components)
+    opt = options(precision, n_slices, p.a_en, p.a_ee, x_components, basis=basis)
     st = Stats()
-    arrs = [p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2, c_sets, m, n, o]
+    aos1, aos2 = (None, None) if basis is not None else (p.aos1, p.aos2)
+    arrs = [p.r1, p.wr1, p.r2, p.wr2, p.rn, aos1, aos2, c_sets, m, n, o]
     s = load().cutc_int_scan(ctypes.byref(opt), ns, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc,
                              p.size_bh, *[_vp(a) for a in arrs],
                              _vp(ae) if ae is not None else None,
@@ -254,6 +283,18 @@ def scan_integrals(p, c_sets, a_en=None, a_ee=None, precision=PLAIN_FP64, n_slic
     if s != CUTC_OK:
         raise CutcError(s, last_error())
     return (X, I, st.as_dict()) if with_stats else (X, I)
+
+
+def eval_aos(shells, r, components=4):
+    """AO values (components=1) or values and gradients (4) of synth shells at the
+    points r (n, 3), on the GPU: C array (components, n_ao, n)."""
+    b = make_basis(shells)
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    out = np.empty((components, b.n_ao, r.shape[0]))
+    s = load().cutc_eval_aos(ctypes.byref(b), r.shape[0], _vp(r), components, _vp(out), 0, None)
+    if s != CUTC_OK:
+        raise CutcError(s, last_error())
+    return out
 
 
 def jast_bh_device(r1, r2, rn, c_bh, m_bh, n_bh, o_bh, G, i0=0, n1b=None,
@@ -319,10 +360,15 @@ class Server:
             raise CutcError(s, last_error())
         self._live = {}
 
-    def submit(self, p, molecule_key=0, precision=PLAIN_FP64, n_slices=None, x_components=3):
+    def submit(self, p, molecule_key=0, precision=PLAIN_FP64, n_slices=None, x_components=3,
+               aos_from_basis=False):
+        """aos_from_basis: send p.shells instead of the AO arrays (evaluated on the GPU)."""
         X = np.empty((x_components, p.n_grid1, p.n_ao ** 2))
         I = np.empty((p.n_ao ** 2, p.n_ao ** 2))
-        arrs = p.arrays()
+        arrs = dict(p.arrays())
+        basis = make_basis(p.shells) if aos_from_basis else None
+        if aos_from_basis:
+            arrs["aos1"] = arrs["aos2"] = None
         q = Request()
         q.molecule_key = molecule_key
         q.n_grid1, q.n_grid2, q.n_ao, q.n_nuc, q.size_bh = (p.n_grid1, p.n_grid2, p.n_ao,
@@ -330,21 +376,21 @@ class Server:
         for k, name in (("r1", "r1"), ("wr1", "wr1"), ("r2", "r2"), ("wr2", "wr2"), ("rn", "rn"),
                         ("aos1", "aos_data1"), ("aos2", "aos_data2"), ("c_bh", "c_bh"),
                         ("m_bh", "m_bh"), ("n_bh", "n_bh"), ("o_bh", "o_bh")):
-            setattr(q, name, arrs[k].ctypes.data)
+            setattr(q, name, arrs[k].ctypes.data if arrs[k] is not None else None)
         q.int2_grad1_u12_ao = X.ctypes.data
         q.int_2e_ao = I.ctypes.data
-        q.options = options(precision, n_slices, p.a_en, p.a_ee, x_components)
+        q.options = options(precision, n_slices, p.a_en, p.a_ee, x_components, basis=basis)
         t = ctypes.c_ulonglong()
         s = load().cutc_server_submit(self._h, ctypes.byref(q), ctypes.byref(t))
         if s != CUTC_OK:
             raise CutcError(s, last_error())
-        self._live[t.value] = (p, X, I, q)
+        self._live[t.value] = (p, X, I, q, basis)
         return t.value
 
     def wait(self, ticket):
         lat = ctypes.c_double()
         s = load().cutc_server_wait(self._h, ticket, ctypes.byref(lat))
-        p, X, I, q = self._live.pop(ticket)
+        p, X, I, q, _ = self._live.pop(ticket)
         if s != CUTC_OK:
             raise CutcError(s, last_error())
         return X, I, lat.value

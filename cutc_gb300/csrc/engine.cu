@@ -26,6 +26,7 @@
 #include <thread>
 #include <vector>
 
+#include "aos.cuh"
 #include "common.cuh"
 #include "engine.cuh"
 #include "pair.cuh"
@@ -301,12 +302,19 @@ static int validate(const Request &R)
         cutc_set_error(CUTC_ERR_INVALID, "n_ao=%d too large", R.nA);
         return CUTC_ERR_INVALID;
     }
-    const void *ptrs[] = {R.r1, R.wr1, R.r2, R.wr2, R.rn, R.aos1, R.aos2, R.X, R.I};
+    const void *ptrs[] = {R.r1, R.wr1, R.r2, R.wr2, R.rn, R.X, R.I};
     for (const void *p : ptrs)
         if (!p) {
             cutc_set_error(CUTC_ERR_INVALID, "NULL array argument");
             return CUTC_ERR_INVALID;
         }
+    if (!R.aos1 || !R.aos2) {
+        if (!R.basis) {
+            cutc_set_error(CUTC_ERR_INVALID, "NULL AO array and no basis to evaluate it from");
+            return CUTC_ERR_INVALID;
+        }
+        CUTC_TRY(validate_basis(R.basis, R.nA));
+    }
     if (R.nB > 0 && (!R.c_bh || !R.m_bh || !R.n_bh || !R.o_bh)) {
         cutc_set_error(CUTC_ERR_INVALID, "NULL Jastrow parameter array");
         return CUTC_ERR_INVALID;
@@ -345,7 +353,7 @@ static int validate(const Request &R)
 enum Slot {
     S_R1, S_WR1, S_R2, S_WR2, S_RN, S_AOS1, S_AOS2, S_COEF, S_EXPS, S_OFF,
     S_T1, S_F2, S_P, S_G, S_XP, S_S0, S_SL, S_H, S_N, S_XOUT, S_XOUT1, S_IOUT, S_IOUT1,
-    S_R2D, S_F2D, S_POLY, S_BLASWS,
+    S_R2D, S_F2D, S_POLY, S_BLASWS, S_BASIS,
     S_SPLIT0  // split-form slots follow
 };
 
@@ -482,9 +490,26 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         CUTC_TRY(put(S_R2, R.r2, 3 * (size_t)n2 * 8, &d_r2));
         CUTC_TRY(put(S_WR2, R.wr2, (size_t)n2 * 8, &d_wr2));
         CUTC_TRY(put(S_RN, R.rn, 3 * (size_t)nN * 8, &d_rn));
-        CUTC_TRY(put(S_AOS1, R.aos1, 4 * (size_t)n1 * nA * 8, &d_aos1));
+        if (R.aos1)
+            CUTC_TRY(put(S_AOS1, R.aos1, 4 * (size_t)n1 * nA * 8, &d_aos1));
         // only the value component of aos_data2 is used (src/long_range_integ.cu:30-35)
-        CUTC_TRY(put(S_AOS2, R.aos2, (size_t)n2 * nA * 8, &d_aos2v));
+        if (R.aos2)
+            CUTC_TRY(put(S_AOS2, R.aos2, (size_t)n2 * nA * 8, &d_aos2v));
+    }
+    if (!R.aos1 || !R.aos2) {
+        // AO values (and r1 gradients) from the basis, on the device
+        BasisDev B;
+        CUTC_TRY(upload_basis(W, S_BASIS, st, R.basis, &B));
+        if (!R.aos1) {
+            CUTC_TRY(W.get(S_AOS1, 4 * (size_t)n1 * nA * 8, &p));
+            CUTC_TRY(launch_eval_aos(st, B, n1, d_r1, 4, (double *)p, n1));
+            d_aos1 = (const double *)p;
+        }
+        if (!R.aos2) {
+            CUTC_TRY(W.get(S_AOS2, (size_t)n2 * nA * 8, &p));
+            CUTC_TRY(launch_eval_aos(st, B, n2, d_r2, 1, (double *)p, n2));
+            d_aos2v = (const double *)p;
+        }
     }
     const int nt = (int)exps.size();
     double *d_coef;
@@ -945,6 +970,7 @@ extern "C" int cutc_int_ex(const cutc_options *opt, int n_grid1, int n_grid2, in
     R.pair_fp64 = opt->pair_fp64;
     R.k_split = opt->k_split;
     R.int2e_layout = opt->int2e_layout;
+    R.basis = opt->basis;
     R.n1 = n_grid1; R.n2 = n_grid2; R.nA = n_ao; R.nN = n_nuc; R.nB = size_bh;
     R.r1 = r1; R.wr1 = wr1; R.r2 = r2; R.wr2 = wr2; R.rn = rn;
     R.aos1 = aos_data1; R.aos2 = aos_data2;
@@ -994,6 +1020,7 @@ extern "C" int cutc_int_scan(const cutc_options *opt, int n_sets, int n_grid1, i
     base.pair_fp64 = opt->pair_fp64;
     base.k_split = opt->k_split;
     base.int2e_layout = opt->int2e_layout;
+    base.basis = opt->basis;
     base.n1 = n_grid1; base.n2 = n_grid2; base.nA = n_ao; base.nN = n_nuc; base.nB = size_bh;
     base.r1 = r1; base.wr1 = wr1; base.r2 = r2; base.wr2 = wr2; base.rn = rn;
     base.aos1 = aos_data1; base.aos2 = aos_data2;
@@ -1001,7 +1028,7 @@ extern "C" int cutc_int_scan(const cutc_options *opt, int n_sets, int n_grid1, i
     cudaStream_t st = base.stream ? base.stream : E->stream;
     if (!opt->device_pointers) {
         // the molecule arrays go to the device once for all parameter sets
-        if (!r1 || !wr1 || !r2 || !wr2 || !rn || !aos_data1 || !aos_data2) {
+        if (!r1 || !wr1 || !r2 || !wr2 || !rn || ((!aos_data1 || !aos_data2) && !opt->basis)) {
             cutc_set_error(CUTC_ERR_INVALID, "NULL array argument");
             return CUTC_ERR_INVALID;
         }
@@ -1012,10 +1039,34 @@ extern "C" int cutc_int_scan(const cutc_options *opt, int n_sets, int n_grid1, i
             {155, aos_data1, 4 * (size_t)n_grid1 * n_ao, &base.aos1},
             {156, aos_data2, (size_t)n_grid2 * n_ao, &base.aos2}};
         for (auto &u : up) {
+            if (!u.src)
+                continue;  // evaluated from the basis below
             void *p = nullptr;
             CUTC_TRY(E->ws.get(u.slot, u.n * sizeof(double), &p));
             CUTC_CUDA_TRY(cudaMemcpyAsync(p, u.src, u.n * sizeof(double), cudaMemcpyHostToDevice, st));
             *u.dst = (const double *)p;
+        }
+        base.in_device = 1;
+    }
+    if (!base.aos1 || !base.aos2) {
+        // every set shares the molecule: evaluate its AOs once
+        if (!opt->basis) {
+            cutc_set_error(CUTC_ERR_INVALID, "NULL AO array and no basis to evaluate it from");
+            return CUTC_ERR_INVALID;
+        }
+        CUTC_TRY(validate_basis(opt->basis, n_ao));
+        BasisDev B;
+        CUTC_TRY(upload_basis(E->ws, 157, st, opt->basis, &B));
+        void *p = nullptr;
+        if (!base.aos1) {
+            CUTC_TRY(E->ws.get(155, 4 * (size_t)n_grid1 * n_ao * sizeof(double), &p));
+            CUTC_TRY(launch_eval_aos(st, B, n_grid1, base.r1, 4, (double *)p, n_grid1));
+            base.aos1 = (const double *)p;
+        }
+        if (!base.aos2) {
+            CUTC_TRY(E->ws.get(156, (size_t)n_grid2 * n_ao * sizeof(double), &p));
+            CUTC_TRY(launch_eval_aos(st, B, n_grid2, base.r2, 1, (double *)p, n_grid2));
+            base.aos2 = (const double *)p;
         }
         base.in_device = 1;
     }
@@ -1113,4 +1164,36 @@ extern "C" void cutc_release(void)
     cudaStreamSynchronize(E->xfer);
     E->ws.release();
     E->pinned.release();
+}
+
+extern "C" int cutc_eval_aos(const cutc_basis *basis, int n_points, const double *r,
+                             int components, double *aos, int device_pointers, void *stream)
+{
+    using namespace cutc;
+    if (n_points < 0 || !r || !aos || (components != 1 && components != 4)) {
+        cutc_set_error(CUTC_ERR_INVALID, "invalid AO evaluation arguments");
+        return CUTC_ERR_INVALID;
+    }
+    CUTC_TRY(validate_basis(basis, basis ? basis->n_ao : 0));
+    Engine *E = nullptr;
+    CUTC_TRY(get_engine(&E));
+    std::lock_guard<std::mutex> lk(E->mu);
+    cudaStream_t st = stream ? (cudaStream_t)stream : E->stream;
+    BasisDev B;
+    CUTC_TRY(upload_basis(E->ws, 160, st, basis, &B));
+    if (n_points == 0)
+        return CUTC_OK;
+    const size_t out_bytes = (size_t)components * basis->n_ao * n_points * sizeof(double);
+    if (device_pointers)
+        return launch_eval_aos(st, B, n_points, r, components, aos, n_points);
+    void *pr = nullptr, *po = nullptr;
+    CUTC_TRY(E->ws.get(161, 3 * (size_t)n_points * sizeof(double), &pr));
+    CUTC_TRY(E->ws.get(162, out_bytes, &po));
+    CUTC_CUDA_TRY(cudaMemcpyAsync(pr, r, 3 * (size_t)n_points * sizeof(double),
+                                  cudaMemcpyHostToDevice, st));
+    CUTC_TRY(launch_eval_aos(st, B, n_points, (const double *)pr, components, (double *)po,
+                             n_points));
+    CUTC_CUDA_TRY(cudaMemcpyAsync(aos, po, out_bytes, cudaMemcpyDeviceToHost, st));
+    CUTC_CUDA_TRY(cudaStreamSynchronize(st));
+    return CUTC_OK;
 }

@@ -71,6 +71,7 @@ struct Request {
     int pair_fp64 = 0;  // split form: FP64 pair terms
     int k_split = 0;    // split form: max K per tensor-core launch (0 = default)
     int int2e_layout = CUTC_INT2E_PQST;
+    const cutc_basis *basis = nullptr;  // evaluates aos1 / aos2 when those are NULL
     uint64_t mol_tag = 0;  // non-zero: molecule arrays identical to earlier builds with this tag
     cudaStream_t stream = nullptr;
     int n1 = 0, n2 = 0, nA = 0, nN = 0, nB = 0;

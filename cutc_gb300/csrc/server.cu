@@ -30,6 +30,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "aos.cuh"
 #include "common.cuh"
 #include "engine.cuh"
 
@@ -187,10 +188,24 @@ static int acquire_molecule(Server *S, Engine *E, const cutc_request &q, MolEntr
             {m->r1, q.r1, 3 * n1}, {m->wr1, q.wr1, n1}, {m->r2, q.r2, 3 * n2}, {m->wr2, q.wr2, n2},
             {m->rn, q.rn, 3 * nN}, {m->aos1, q.aos_data1, 4 * n1 * nA}, {m->aos2v, q.aos_data2, n2 * nA}};
         for (auto &c : cp)
-            if (e == cudaSuccess)
+            if (e == cudaSuccess && c.src)  // AO arrays may come from the basis
                 e = cudaMemcpyAsync(c.dst, c.src, c.n * sizeof(double), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess)
-            e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cutc_set_error(CUTC_ERR_CUDA, "molecule upload: %s", cudaGetErrorString(e));
+            return finish(CUTC_ERR_CUDA);
+        }
+        if (!q.aos_data1 || !q.aos_data2) {
+            BasisDev B;
+            int s = upload_basis(E->ws, 170, st, q.options.basis, &B);
+            if (s == CUTC_OK && !q.aos_data1)
+                s = launch_eval_aos(st, B, q.n_grid1, m->r1, 4, m->aos1, q.n_grid1);
+            if (s == CUTC_OK && !q.aos_data2)
+                s = launch_eval_aos(st, B, q.n_grid2, m->r2, 1, m->aos2v, q.n_grid2);
+            if (s != CUTC_OK)
+                return finish(s);
+        }
+        e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
             cudaGetLastError();
             cutc_set_error(CUTC_ERR_CUDA, "molecule upload: %s", cudaGetErrorString(e));
@@ -229,6 +244,7 @@ static Request to_request(const cutc_request &q)
     R.pair_fp64 = o.pair_fp64;
     R.k_split = o.k_split;
     R.int2e_layout = o.int2e_layout;
+    R.basis = o.basis;
     R.n1 = q.n_grid1; R.n2 = q.n_grid2; R.nA = q.n_ao; R.nN = q.n_nuc; R.nB = q.size_bh;
     R.r1 = q.r1; R.wr1 = q.wr1; R.r2 = q.r2; R.wr2 = q.wr2; R.rn = q.rn;
     R.aos1 = q.aos_data1; R.aos2 = q.aos_data2;
@@ -376,6 +392,8 @@ extern "C" int cutc_server_submit(cutc_server *h, const cutc_request *req, unsig
         cutc_set_error(CUTC_ERR_INVALID, "NULL argument");
         return CUTC_ERR_INVALID;
     }
+    if ((!req->aos_data1 || !req->aos_data2))
+        CUTC_TRY(validate_basis(req->options.basis, req->n_ao));
     auto job = std::make_unique<Job>();
     job->req = *req;
     Request R = to_request(*req);

@@ -58,6 +58,7 @@ class Problem:
     o_bh: np.ndarray
     a_en: float = 1.0
     a_ee: float = 1.0
+    shells: list | None = None  # the basis aos1 / aos2 were evaluated from
 
     @property
     def n_grid1(self) -> int:
@@ -212,6 +213,25 @@ def eval_aos(shells: list[Shell], r: np.ndarray) -> np.ndarray:
     return out
 
 
+def basis_arrays(shells: list[Shell]) -> dict:
+    """The basis one entry per AO, as the engine's cutc_basis takes it: C arrays
+    center (nA, 3), power (nA, 3) int32, prim_offset (nA + 1,) int32, prim_exp and
+    prim_coef (primitives of AO a at prim_offset[a] .. prim_offset[a + 1] - 1)."""
+    center, power, off, ex, co = [], [], [0], [], []
+    for s in shells:
+        for comp in s.comps:
+            center.append(s.center)
+            power.append(comp)
+            ex.extend(s.exps)
+            co.extend(s.coefs)
+            off.append(len(ex))
+    return dict(center=np.ascontiguousarray(np.array(center, dtype=np.float64).reshape(-1, 3)),
+                power=np.ascontiguousarray(np.array(power, dtype=np.int32).reshape(-1, 3)),
+                prim_offset=np.ascontiguousarray(np.array(off, dtype=np.int32)),
+                prim_exp=np.ascontiguousarray(np.array(ex, dtype=np.float64)),
+                prim_coef=np.ascontiguousarray(np.array(co, dtype=np.float64)))
+
+
 EXP_CHOICES = np.array([0, 2, 3, 4], dtype=np.int32)
 
 
@@ -237,7 +257,7 @@ def make_problem(n_nuc: int, n_ao: int, n_grid1: int, n_grid2: int, size_bh: int
     aos1 = eval_aos(shells, r1)
     aos2 = eval_aos(shells, r2)
     c, m, nn, o = make_jastrow(n_nuc, size_bh, rng, sigma)
-    return Problem(r1, wr1, r2, wr2, rn, aos1, aos2, c, m, nn, o, a_en, a_ee)
+    return Problem(r1, wr1, r2, wr2, rn, aos1, aos2, c, m, nn, o, a_en, a_ee, shells)
 
 
 # Named workloads (sizes of the measured configurations).

@@ -56,6 +56,20 @@ int cutc_int(int nxBlocks, int nyBlocks, int nzBlocks,
              double *int2_grad1_u12_ao, double *int_2e_ao);
 
 /* ---- extended API (no reference counterpart) --------------------------- */
+
+/* A Cartesian Gaussian basis, one entry per atomic orbital (host memory):
+ *   chi_a(r) = x^lx y^ly z^lz sum_k c_k exp(-alpha_k |r - C_a|^2),  (x,y,z) = r - C_a,
+ * with k = prim_offset[a] .. prim_offset[a+1]-1, normalisation folded into
+ * c_k, powers 0..8, 1..64 primitives per function. */
+typedef struct cutc_basis {
+    int n_ao;
+    const double *center;       /* (3, n_ao): C_a */
+    const int *power;           /* (3, n_ao): lx, ly, lz */
+    const int *prim_offset;     /* (n_ao + 1), prim_offset[0] = 0 */
+    const double *prim_exp;     /* alpha_k */
+    const double *prim_coef;    /* c_k */
+} cutc_basis;
+
 typedef struct cutc_options {
     int precision;          /* CUTC_PLAIN_FP64 or CUTC_SPLIT_BF16 */
     int n_slices;           /* split form: BF16 slices per operand, 3..7 (default 5) */
@@ -71,6 +85,8 @@ typedef struct cutc_options {
     int int2e_layout;       /* CUTC_INT2E_PQST (reference order) or CUTC_INT2E_PSQT: int_2e with
                                its 2nd and 3rd indices swapped, as trans_pqst_psqt_inplace
                                leaves it (the order cutc_no uses), written directly */
+    const cutc_basis *basis;    /* with aos_data1 and/or aos_data2 NULL: those AO arrays are
+                                   evaluated on the device from this basis (NULL: not used) */
 } cutc_options;
 
 #define CUTC_INT2E_PQST 0
@@ -229,6 +245,15 @@ int cutc_server_wait(cutc_server *server, unsigned long long ticket, double *lat
 int cutc_server_get_stats(cutc_server *server, cutc_server_stats *stats);
 /* Finishes the queued requests, then frees the contexts and the cache. */
 void cutc_server_destroy(cutc_server *server);
+
+/* AO values (components = 1) or values and gradients (components = 4) of the
+ * basis at n_points points r(3, n_points), written as aos(n_points, n_ao,
+ * components) column-major: the layout of aos_data1 / aos_data2.  r and aos are
+ * device pointers when device_pointers is 1 (then the call is asynchronous on
+ * stream), host pointers otherwise.  No reference counterpart (the reference
+ * takes AO values from its caller). */
+int cutc_eval_aos(const cutc_basis *basis, int n_points, const double *r, int components,
+                  double *aos, int device_pointers, void *stream);
 
 /* ---- reference helpers with the reference's names and semantics ------------
  * Device pointers; launched on the legacy default stream without a host
