@@ -33,7 +33,7 @@ EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_int_scan", "cutc_default_options", "
            "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_validate_launch_dims",
            "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
            "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy",
-           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos"]
+           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos", "cutc_x_ao_to_mo"]
 
 INT2E_PQST = 0
 INT2E_PSQT = 1
@@ -151,6 +151,8 @@ def load(path: str = LIB_PATH):
     L.trans_pqst_psqt_copy.restype = None
     L.cutc_eval_aos.argtypes = [ctypes.POINTER(Basis), i, vp, i, vp, i, vp]
     L.cutc_eval_aos.restype = i
+    L.cutc_x_ao_to_mo.argtypes = [i, i, i, i, vp, vp, vp, vp, i, vp]
+    L.cutc_x_ao_to_mo.restype = i
     L.cutc_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
     L.cutc_server_default_config.restype = None
     L.cutc_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
@@ -292,6 +294,30 @@ def eval_aos(shells, r, components=4):
     r = np.ascontiguousarray(r, dtype=np.float64)
     out = np.empty((components, b.n_ao, r.shape[0]))
     s = load().cutc_eval_aos(ctypes.byref(b), r.shape[0], _vp(r), components, _vp(out), 0, None)
+    if s != CUTC_OK:
+        raise CutcError(s, last_error())
+    return out
+
+
+def x_ao_to_mo(X_ao, mo_l, mo_r):
+    """X in the MO basis in cutc_no's order: X_ao is the C array (comps, n1, nA, nA)
+    that build_integrals returns, mo_l and mo_r the C arrays (n_mo, nA) (Fortran
+    (nA, n_mo) coefficients).  Returns the C array (n_mo, n_mo, comps, n1), i.e.
+    Fortran x_mo(n1, comps, n_mo, n_mo); works on host arrays or CUDA tensors."""
+    comps, n1 = X_ao.shape[0], X_ao.shape[1]
+    nA = mo_l.shape[1]  # X_ao may also be (comps, n1, nA^2), as build_integrals returns it
+    if X_ao.shape[2:] not in ((nA, nA), (nA * nA,)):
+        raise ValueError("X_ao does not match the coefficients' n_ao")
+    n_mo = mo_l.shape[0]
+    dev = hasattr(X_ao, "data_ptr")
+    if dev:
+        import torch
+        out = torch.empty((n_mo, n_mo, comps, n1), dtype=torch.float64, device=X_ao.device)
+    else:
+        X_ao, mo_l, mo_r = (np.ascontiguousarray(a, dtype=np.float64) for a in (X_ao, mo_l, mo_r))
+        out = np.empty((n_mo, n_mo, comps, n1))
+    s = load().cutc_x_ao_to_mo(n1, nA, n_mo, comps, _vp(mo_l), _vp(mo_r), _vp(X_ao), _vp(out),
+                               1 if dev else 0, None)
     if s != CUTC_OK:
         raise CutcError(s, last_error())
     return out

@@ -255,6 +255,18 @@ void cutc_server_destroy(cutc_server *server);
 int cutc_eval_aos(const cutc_basis *basis, int n_points, const double *r, int components,
                   double *aos, int device_pointers, void *stream);
 
+/* X in the MO basis, in the order the reference's cutc_no reads it
+ * (src/no_tmpJ_cs_kernel.cu:18-30):
+ *   x_mo(g, m, i, j) = sum_{a,b} mo_l_coef(a, i) x_ao(a, b, g, m) mo_r_coef(b, j)
+ * x_ao(n_ao, n_ao, n_grid1, components) as cutc_int writes it, mo_l_coef and
+ * mo_r_coef (n_ao, n_mo), x_mo(n_grid1, components, n_mo, n_mo), all column-major
+ * FP64, components 3 or 4.  Device pointers when device_pointers is 1 (then
+ * asynchronous on stream), host pointers otherwise.  No reference counterpart
+ * (the reference's workflow does this step outside the library). */
+int cutc_x_ao_to_mo(int n_grid1, int n_ao, int n_mo, int components,
+                    const double *mo_l_coef, const double *mo_r_coef,
+                    const double *x_ao, double *x_mo, int device_pointers, void *stream);
+
 /* ---- reference helpers with the reference's names and semantics ------------
  * Device pointers; launched on the legacy default stream without a host
  * synchronisation, as the reference does; errors are recorded for
