@@ -715,6 +715,9 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
             P.a_ee_hi = (float)R.a_ee;
             P.a_ee_lo = (float)(R.a_ee - (double)P.a_ee_hi);
             P.G = reinterpret_cast<float2 *>(d_G); P.ldg = n2; P.plane = (int64_t)nb * n2;
+            // the kernel also leaves the row maxima the G slicer needs
+            CUTC_CUDA_TRY(cudaMemsetAsync(sp.BX.rmax, 0, 4 * (size_t)nb * 8, st));
+            P.rmax = sp.BX.rmax;
             CUTC_TRY(launch_pair_df(st, P, pexp, psparse, d_rn, R.a_en));
             note_launches(3);
         }
@@ -733,7 +736,7 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
                 CUTC_CUDA_TRY(cudaEventRecord(tev[3], st));
         } else {
             CUTC_TRY(split_x_tile(E, R, st, sp, reinterpret_cast<const float2 *>(d_G), nb, d_Xt,
-                                  tev ? tev[2] : nullptr, tev ? tev[3] : nullptr));
+                                  tev ? tev[2] : nullptr, tev ? tev[3] : nullptr, !R.pair_fp64));
         }
 
         // the tile's share of int_2e (src/build_int_2e_ao.cu:60-67 and 97-104, packed):

@@ -50,6 +50,9 @@ struct PairDfArgs {
     float2 *G;              // G[c * plane + i * ldg + j] as (hi, lo)
     int64_t ldg;
     int64_t plane;
+    // optional: rmax[c * n1b + i] |= bits of max_j |G| (only its exponent field is
+    // exact: it is the max of the high 32 bits), for the split slicer
+    unsigned long long *rmax = nullptr;
 };
 
 int pair_df_max_exp(const int *exps, int n_terms);

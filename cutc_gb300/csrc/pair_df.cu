@@ -210,92 +210,110 @@ pair_df_kernel(PairDfArgs P)
         const df::D dz = df::sub(df::make(rr[2].x, rr[2].y), df::make(z2.x, z2.y));
         const df::D d2 = df::add(df::add(df::sqr(dx), df::sqr(dy)), df::sqr(dz));
         const int64_t o = (int64_t)(row0 + r) * P.ldg + j;
+        float2 w4[4];
         if (d2.hi < kNearR2) {
             double v[4];
             pair_fp64_single(P, row0 + r, j, v);
             for (int c = 0; c < 4; c++) {
                 const df::D w = df::from_double(v[c]);
-                P.G[o + c * P.plane] = make_float2(w.hi, w.lo);
+                w4[c] = make_float2(w.hi, w.lo);
             }
-            continue;
-        }
-        // g = a r / (1 + a r), grad g = a / (r (1 + a r)^2) (r1 - r2)
-        const df::D rd = df::sqrt(d2);
-        const df::D ar = df::mul(rd, a);
-        const df::D t = df::recip(df::add_f(ar, 1.0f));
-        const df::D g = df::mul(ar, t);
-        const df::D s = df::mul(df::mul(df::sqr(t), a), df::recip(rd));
-        const df::D gx = df::mul(s, dx), gy = df::mul(s, dy), gz = df::mul(s, dz);
+        } else {
+            // g = a r / (1 + a r), grad g = a / (r (1 + a r)^2) (r1 - r2)
+            const df::D rd = df::sqrt(d2);
+            const df::D ar = df::mul(rd, a);
+            const df::D t = df::recip(df::add_f(ar, 1.0f));
+            const df::D g = df::mul(ar, t);
+            const df::D s = df::mul(df::mul(df::sqr(t), a), df::recip(rd));
+            const df::D gx = df::mul(s, dx), gy = df::mul(s, dy), gz = df::mul(s, dz);
 
-        df::D ux = {0.f, 0.f}, uy = {0.f, 0.f}, uz = {0.f, 0.f}, dudg = {0.f, 0.f};
-        const float2 *cr = s_coef + r * per_row;
-        if constexpr (Sp) {
-            const df::D g2 = df::sqr(g);
+            df::D ux = {0.f, 0.f}, uy = {0.f, 0.f}, uz = {0.f, 0.f}, dudg = {0.f, 0.f};
+            const float2 *cr = s_coef + r * per_row;
+            if constexpr (Sp) {
+                const df::D g2 = df::sqr(g);
+                for (int A = 0; A < P.nN; A++) {
+                    const float2 f2v = P.f2d[(int64_t)A * P.n2 + j];
+                    const df::D f2 = df::make(f2v.x, f2v.y);
+                    const df::D f22 = df::sqr(f2);
+                    const float2 *U = cr + A * L::kN;
+                    const float2 *W = U + L::kU;
+                    auto u = [&](int b, int o) { return df::make(U[b * 5 + o].x, U[b * 5 + o].y); };
+                    auto w = [&](int b, int o) { return df::make(W[b * 4 + o].x, W[b * 4 + o].y); };
+                    auto pu = [&](int b) {
+                        return df::fma(df::fma(df::fma(u(b, 4), g, u(b, 3)), g, u(b, 2)), g2, u(b, 0));
+                    };
+                    auto pw = [&](int b) { return df::fma(df::fma(w(b, 3), g, w(b, 2)), g, w(b, 1)); };
+                    const df::D acc =
+                        df::fma(df::fma(df::fma(pu(4), f2, pu(3)), f2, pu(2)), f22, pu(0));
+                    const df::D acw =
+                        df::fma(df::fma(df::fma(pw(4), f2, pw(3)), f2, pw(2)), f22, pw(0));
+                    const float2 *gf = W + L::kW;
+                    ux = df::fma(acc, df::make(gf[0].x, gf[0].y), ux);
+                    uy = df::fma(acc, df::make(gf[1].x, gf[1].y), uy);
+                    uz = df::fma(acc, df::make(gf[2].x, gf[2].y), uz);
+                    dudg = df::add(dudg, acw);
+                }
+                dudg = df::mul(dudg, g);
+            } else {
             for (int A = 0; A < P.nN; A++) {
                 const float2 f2v = P.f2d[(int64_t)A * P.n2 + j];
                 const df::D f2 = df::make(f2v.x, f2v.y);
-                const df::D f22 = df::sqr(f2);
                 const float2 *U = cr + A * L::kN;
                 const float2 *W = U + L::kU;
-                auto u = [&](int b, int o) { return df::make(U[b * 5 + o].x, U[b * 5 + o].y); };
-                auto w = [&](int b, int o) { return df::make(W[b * 4 + o].x, W[b * 4 + o].y); };
-                auto pu = [&](int b) {
-                    return df::fma(df::fma(df::fma(u(b, 4), g, u(b, 3)), g, u(b, 2)), g2, u(b, 0));
-                };
-                auto pw = [&](int b) { return df::fma(df::fma(w(b, 3), g, w(b, 2)), g, w(b, 1)); };
-                const df::D acc =
-                    df::fma(df::fma(df::fma(pu(4), f2, pu(3)), f2, pu(2)), f22, pu(0));
-                const df::D acw =
-                    df::fma(df::fma(df::fma(pw(4), f2, pw(3)), f2, pw(2)), f22, pw(0));
+                // du/df1A = sum_b f2^b (sum_o U[b][o] g^o)
+                df::D acc = {0.f, 0.f};
+    #pragma unroll
+                for (int b = E; b >= 0; b--) {
+                    df::D in = df::make(U[b * (E + 1) + E].x, U[b * (E + 1) + E].y);
+    #pragma unroll
+                    for (int q = E - 1; q >= 0; q--)
+                        in = df::fma(in, g, df::make(U[b * (E + 1) + q].x, U[b * (E + 1) + q].y));
+                    acc = (b == E) ? in : df::fma(acc, f2, in);
+                }
+                // du/dg contribution = sum_b f2^b (sum_o' W[b][o'] g^o')
+                df::D acw = {0.f, 0.f};
+    #pragma unroll
+                for (int b = E; b >= 0; b--) {
+                    df::D in = df::make(W[b * E + E - 1].x, W[b * E + E - 1].y);
+    #pragma unroll
+                    for (int q = E - 2; q >= 0; q--)
+                        in = df::fma(in, g, df::make(W[b * E + q].x, W[b * E + q].y));
+                    acw = (b == E) ? in : df::fma(acw, f2, in);
+                }
                 const float2 *gf = W + L::kW;
                 ux = df::fma(acc, df::make(gf[0].x, gf[0].y), ux);
                 uy = df::fma(acc, df::make(gf[1].x, gf[1].y), uy);
                 uz = df::fma(acc, df::make(gf[2].x, gf[2].y), uz);
                 dudg = df::add(dudg, acw);
             }
-            dudg = df::mul(dudg, g);
-        } else {
-        for (int A = 0; A < P.nN; A++) {
-            const float2 f2v = P.f2d[(int64_t)A * P.n2 + j];
-            const df::D f2 = df::make(f2v.x, f2v.y);
-            const float2 *U = cr + A * L::kN;
-            const float2 *W = U + L::kU;
-            // du/df1A = sum_b f2^b (sum_o U[b][o] g^o)
-            df::D acc = {0.f, 0.f};
-#pragma unroll
-            for (int b = E; b >= 0; b--) {
-                df::D in = df::make(U[b * (E + 1) + E].x, U[b * (E + 1) + E].y);
-#pragma unroll
-                for (int q = E - 1; q >= 0; q--)
-                    in = df::fma(in, g, df::make(U[b * (E + 1) + q].x, U[b * (E + 1) + q].y));
-                acc = (b == E) ? in : df::fma(acc, f2, in);
             }
-            // du/dg contribution = sum_b f2^b (sum_o' W[b][o'] g^o')
-            df::D acw = {0.f, 0.f};
+            ux = df::fma(dudg, gx, ux);
+            uy = df::fma(dudg, gy, uy);
+            uz = df::fma(dudg, gz, uz);
+            const df::D n2v = df::add(df::add(df::sqr(ux), df::sqr(uy)), df::sqr(uz));
+            const df::D l = df::mul_f(n2v, -0.5f);
+            w4[0] = make_float2(ux.hi, ux.lo);
+            w4[1] = make_float2(uy.hi, uy.lo);
+            w4[2] = make_float2(uz.hi, uz.lo);
+            w4[3] = make_float2(l.hi, l.lo);
+        }
 #pragma unroll
-            for (int b = E; b >= 0; b--) {
-                df::D in = df::make(W[b * E + E - 1].x, W[b * E + E - 1].y);
+        for (int c = 0; c < 4; c++)
+            P.G[o + c * P.plane] = w4[c];
+        if (P.rmax) {
+            // row maxima for the slicer: the exponent of max |G| is that of the
+            // largest high word; one atomic per converged lane group and row
+            const unsigned mask = __activemask();
+            const bool leader = (int)(threadIdx.x & 31) == __ffs(mask) - 1;
 #pragma unroll
-                for (int q = E - 2; q >= 0; q--)
-                    in = df::fma(in, g, df::make(W[b * E + q].x, W[b * E + q].y));
-                acw = (b == E) ? in : df::fma(acw, f2, in);
+            for (int c = 0; c < 4; c++) {
+                const double v = fabs((double)w4[c].x + (double)w4[c].y);
+                const unsigned hw = (unsigned)((unsigned long long)__double_as_longlong(v) >> 32);
+                const unsigned m = __reduce_max_sync(mask, hw);
+                if (leader && m)
+                    atomicMax(&P.rmax[(int64_t)c * P.n1b + row0 + r], (unsigned long long)m << 32);
             }
-            const float2 *gf = W + L::kW;
-            ux = df::fma(acc, df::make(gf[0].x, gf[0].y), ux);
-            uy = df::fma(acc, df::make(gf[1].x, gf[1].y), uy);
-            uz = df::fma(acc, df::make(gf[2].x, gf[2].y), uz);
-            dudg = df::add(dudg, acw);
         }
-        }
-        ux = df::fma(dudg, gx, ux);
-        uy = df::fma(dudg, gy, uy);
-        uz = df::fma(dudg, gz, uz);
-        const df::D n2v = df::add(df::add(df::sqr(ux), df::sqr(uy)), df::sqr(uz));
-        const df::D l = df::mul_f(n2v, -0.5f);
-        P.G[o] = make_float2(ux.hi, ux.lo);
-        P.G[o + P.plane] = make_float2(uy.hi, uy.lo);
-        P.G[o + 2 * P.plane] = make_float2(uz.hi, uz.lo);
-        P.G[o + 3 * P.plane] = make_float2(l.hi, l.lo);
     }
 }
 

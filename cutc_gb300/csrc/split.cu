@@ -478,24 +478,37 @@ __device__ __forceinline__ void split_digits(double x, int e, __nv_bfloat16 (&ou
 }
 
 // slices[(s * Mpad + r) * Kpad + k] for r < Mpad, k < Kpad (zeros outside M x K);
-// ex[r] = row exponent.
+// ex[r] = row exponent.  Four consecutive k per thread (Kpad is a multiple of 32),
+// so each slice plane gets one 8-byte store per thread.
 template <int S, class Src>
 __global__ void slice_kernel(Src src, int M, int64_t K, int64_t Kpad, int Mpad,
                              const unsigned long long *rmax, __nv_bfloat16 *slices, int *ex)
 {
     const int r = blockIdx.y;
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
     if (k >= Kpad)
         return;
     const int e = r < M ? row_exponent(rmax[r]) : 0;
     if (k == 0)
         ex[r] = e;
-    __nv_bfloat16 d[S];
-    const double x = (r < M && k < K) ? src(r, k) : 0.0;
-    split_digits<S>(x, e, d);
+    __nv_bfloat16 d[4][S];
 #pragma unroll
-    for (int s = 0; s < S; s++)
-        slices[((int64_t)s * Mpad + r) * Kpad + k] = d[s];
+    for (int q = 0; q < 4; q++) {
+        const double x = (r < M && k + q < K) ? src(r, k + q) : 0.0;
+        split_digits<S>(x, e, d[q]);
+    }
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+        __nv_bfloat162 lo, hi;
+        lo.x = d[0][s];
+        lo.y = d[1][s];
+        hi.x = d[2][s];
+        hi.y = d[3][s];
+        uint2 w;
+        w.x = *reinterpret_cast<unsigned *>(&lo);
+        w.y = *reinterpret_cast<unsigned *>(&hi);
+        *reinterpret_cast<uint2 *>(slices + ((int64_t)s * Mpad + r) * Kpad + k) = w;
+    }
 }
 
 // Same for a matrix stored column by column, src[(k0 + k) * ld + r], through a
@@ -599,25 +612,33 @@ static int alloc_operand(Workspace &W, int slot, int S, int M, int row_mult, int
     return CUTC_OK;
 }
 
+// have_rmax: op.rmax already holds the row maxima (written by the producer of src)
 template <int S, class Src>
-static int slice_rows(cudaStream_t st, Src src, Operand &op)
+static int slice_rows(cudaStream_t st, Src src, Operand &op, bool have_rmax = false)
 {
-    CUTC_CUDA_TRY(cudaMemsetAsync(op.rmax, 0, (size_t)op.Mpad * 8, st));
-    if (op.M > 0 && op.K > 0) {
-        const int64_t kper = 16384;
-        dim3 g1((unsigned)op.M, ceil_div(op.K, kper));
-        rowmax_kernel<Src><<<g1, 256, 0, st>>>(src, op.M, op.K, kper, op.rmax);
-        CUTC_CUDA_TRY(cudaGetLastError());
+    if (!have_rmax) {
+        CUTC_CUDA_TRY(cudaMemsetAsync(op.rmax, 0, (size_t)op.Mpad * 8, st));
+        if (op.M > 0 && op.K > 0) {
+            const int64_t kper = 16384;
+            dim3 g1((unsigned)op.M, ceil_div(op.K, kper));
+            rowmax_kernel<Src><<<g1, 256, 0, st>>>(src, op.M, op.K, kper, op.rmax);
+            CUTC_CUDA_TRY(cudaGetLastError());
+        }
     }
     if (op.Mpad > 65535) {
         cutc_set_error(CUTC_ERR_INVALID, "operand with %d rows exceeds the slicer grid", op.Mpad);
         return CUTC_ERR_INVALID;
     }
-    dim3 g2(ceil_div(op.Kpad, 256), (unsigned)op.Mpad);
+    if (op.Kpad % 4) {
+        cutc_set_error(CUTC_ERR_INVALID, "operand K padding %lld is not a multiple of 4",
+                       (long long)op.Kpad);
+        return CUTC_ERR_INVALID;
+    }
+    dim3 g2(ceil_div(op.Kpad, 4 * 256), (unsigned)op.Mpad);
     slice_kernel<S, Src><<<g2, 256, 0, st>>>(src, op.M, op.K, op.Kpad, op.Mpad, op.rmax,
                                              (__nv_bfloat16 *)op.sl, op.ex);
     CUTC_CUDA_TRY(cudaGetLastError());
-    note_launches(2);
+    note_launches(have_rmax ? 1 : 2);
     return CUTC_OK;
 }
 
@@ -769,7 +790,7 @@ int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *
 }
 
 int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const float2 *G,
-                 int nb, double *Xt, cudaEvent_t gemm_begin, cudaEvent_t gemm_end)
+                 int nb, double *Xt, cudaEvent_t gemm_begin, cudaEvent_t gemm_end, bool have_rmax)
 {
     (void)E;
     SplitPlan &S_ = sp;
@@ -779,7 +800,7 @@ int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, co
     const int64_t np = n_pairs(R.nA);
     SrcDenseDF src{G, (int64_t)R.n2};
     CUTC_SLICES_DISPATCH(sp.n_slices, {
-        CUTC_TRY((slice_rows<S, SrcDenseDF>(st, src, B)));
+        CUTC_TRY((slice_rows<S, SrcDenseDF>(st, src, B, have_rmax)));
         if (gemm_begin)
             CUTC_CUDA_TRY(cudaEventRecord(gemm_begin, st));
         CUTC_TRY((gemm<S>(st, S_.AX, B, 1.0, Xt, np, B.M, 0, 0, 0, S_.err, R.k_split)));

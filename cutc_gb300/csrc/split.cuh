@@ -38,8 +38,10 @@ size_t split_fixed_bytes(const Request &R);
 int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *wr2,
                     const double *aos2v, int64_t n1t, int slot0, SplitPlan &sp);
 // X of one r1 tile: Xt[(m nb + i) np + p] from the df tile G[c][i][j] ((hi, lo) pairs).
+// have_rmax: the row maxima of G are already in sp.BX.rmax (rows c nb + i)
 int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const float2 *G,
-                 int nb, double *Xt, cudaEvent_t gemm_begin, cudaEvent_t gemm_end);
+                 int nb, double *Xt, cudaEvent_t gemm_begin, cudaEvent_t gemm_end,
+                 bool have_rmax = false);
 // Adds the r1 tile's share of the int_2e contractions to H and N (overwrites when
 // first): wr1 and aos1 point at the tile's first row, ld1 is the row stride of aos1.
 int split_int2e_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
