@@ -70,7 +70,9 @@ class Problem:
 
     @property
     def n_ao(self) -> int:
-        return self.aos1.shape[1]
+        if self.aos1 is not None:
+            return self.aos1.shape[1]
+        return sum(len(s.comps) for s in self.shells)
 
     @property
     def n_nuc(self) -> int:
@@ -248,14 +250,16 @@ def make_jastrow(n_nuc: int, size_bh: int, rng: np.random.Generator,
 
 def make_problem(n_nuc: int, n_ao: int, n_grid1: int, n_grid2: int, size_bh: int,
                  seed: int, box: float = 3.0, a_en: float = 1.0, a_ee: float = 1.0,
-                 sigma: float = 0.3) -> Problem:
+                 sigma: float = 0.3, with_aos: bool = True) -> Problem:
+    """with_aos=False leaves aos1 / aos2 as None: the basis (shells) is kept for the
+    engine to evaluate the AOs on the device."""
     rng = np.random.default_rng(seed)
     rn = make_nuclei(n_nuc, box, rng)
     r1, wr1 = make_grid(rn, n_grid1, rng)
     r2, wr2 = make_grid(rn, n_grid2, rng)
     shells = make_basis(rn, n_ao, rng)
-    aos1 = eval_aos(shells, r1)
-    aos2 = eval_aos(shells, r2)
+    aos1 = eval_aos(shells, r1) if with_aos else None
+    aos2 = eval_aos(shells, r2) if with_aos else None
     c, m, nn, o = make_jastrow(n_nuc, size_bh, rng, sigma)
     return Problem(r1, wr1, r2, wr2, rn, aos1, aos2, c, m, nn, o, a_en, a_ee, shells)
 
