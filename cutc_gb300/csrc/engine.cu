@@ -395,27 +395,61 @@ static size_t fixed_bytes(const Request &R)
     return (size_t)b;
 }
 
-// Device bytes per r1 row of a tile: G, the packed X rows, per-point terms,
-// output staging (two buffers) and the r1 operands of the int_2e contraction.
+// Device bytes per r1 row of an X tile: G, per-point terms, output staging (two
+// buffers) and, split form, G's slices and polynomial coefficients.
 static size_t r1_row_bytes(const Request &R)
 {
-    const int64_t np = n_pairs(R.nA), nl = std::max<int64_t>(1, n_strict_pairs(R.nA));
-    size_t b = 4 * (size_t)R.n2 * 8 + 4 * (size_t)np * 8 + (size_t)R.nN * sizeof(NucTerm);
+    size_t b = 4 * (size_t)R.n2 * 8 + (size_t)R.nN * sizeof(NucTerm);
     if (!(R.device_pointers || R.out_device))
         b += 2 * (size_t)R.x_components * R.nA * R.nA * 8;
+    if (R.precision == CUTC_SPLIT_BF16)
+        b += split_r1_row_bytes(R) + pair_df_poly_bytes(6, 1, R.nN);
+    return b;
+}
+
+// Device bytes per r1 row of an int_2e block: the packed X rows and the block's
+// r1 operands of the int_2e contractions.
+static size_t int2e_row_bytes(const Request &R)
+{
+    const int64_t np = n_pairs(R.nA), nl = std::max<int64_t>(1, n_strict_pairs(R.nA));
+    size_t b = 4 * (size_t)np * 8;
     if (R.precision == CUTC_PLAIN_FP64)
         b += ((size_t)np + 3 * (size_t)nl) * 8;
     else
-        b += split_r1_row_bytes(R) + pair_df_poly_bytes(6, 1, R.nN);
+        b += split_int2e_row_bytes(R);
     return b;
+}
+
+// r1 rows per X tile and per int_2e block for a budget (each gets the budget): the
+// int_2e contractions run once per block, with K = its rows, so the block is made
+// as large as its budget allows and cut into equal X tiles that each fit theirs.
+// CUTC_TILE_ROWS / CUTC_INT2E_ROWS cap them.
+static void plan_rows(const Request &R, size_t budget, int64_t *n1t, int64_t *kb)
+{
+    const int64_t n1 = R.n1;
+    int64_t t = std::max<int64_t>(1, std::min<int64_t>((int64_t)(budget / r1_row_bytes(R)), n1));
+    if (R.tile_rows > 0)
+        t = std::min<int64_t>(t, R.tile_rows);
+    int64_t k = std::max<int64_t>(1, std::min<int64_t>((int64_t)(budget / int2e_row_bytes(R)), n1));
+    if (R.int2e_rows > 0)
+        k = std::min<int64_t>(k, R.int2e_rows);
+    const int64_t per = (k + t - 1) / t;  // tiles per block
+    if (k >= n1) {
+        *kb = n1;
+        *n1t = (n1 + per - 1) / per;
+    } else {
+        *n1t = k / per;
+        *kb = per * *n1t;
+    }
 }
 
 size_t build_footprint(const Request &R, size_t tile_budget)
 {
     const int64_t n1 = R.n1, n2 = R.n2, nA = R.nA, nN = R.nN;
-    const size_t row = r1_row_bytes(R);
-    const int64_t n1t = std::max<int64_t>(1, std::min<int64_t>(n1, (int64_t)(tile_budget / row)));
-    double b = (double)fixed_bytes(R) + (double)n1t * row;
+    int64_t n1t, kb;
+    plan_rows(R, tile_budget, &n1t, &kb);
+    double b = (double)fixed_bytes(R) + (double)n1t * r1_row_bytes(R) +
+               (double)kb * int2e_row_bytes(R);
     if (!(R.device_pointers || R.in_device))
         b += (4.0 * n1 + 4.0 * n2 + 3.0 * nN + 4.0 * n1 * nA + (double)n2 * nA) * 8;
     return (size_t)(b * 1.05) + ((size_t)64 << 20);
@@ -528,23 +562,22 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[1], st));
 
     // ---- r1 tiling ---------------------------------------------------------
-    // Every r1 tile is carried all the way: pair terms, its X rows (written
-    // out), and its share of the int_2e contractions, accumulated in FP64 in
-    // H and N.  Device memory is the fixed part plus one tile.
-    const size_t row_bytes = r1_row_bytes(R);
+    // Every r1 tile is carried all the way: pair terms, then its X rows, written
+    // out and kept in the int_2e block buffer.  When a block of whole tiles is
+    // complete, its share of the int_2e contractions (K = its rows) is added to H
+    // and N in FP64.  Device memory is the fixed part plus one tile and one block,
+    // each within the budget.
     size_t budget = R.max_work_bytes;
     if (budget == 0) {
         size_t free_b = 0, total_b = 0;
         CUTC_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
-        budget = std::min<size_t>((size_t)24 << 30, free_b / 3);
+        budget = std::min<size_t>((size_t)24 << 30, free_b / 4);
         const size_t fixed = fixed_bytes(R);
         if (free_b > fixed)
-            budget = std::min<size_t>(budget, (size_t)((double)(free_b - fixed) * 0.8));
+            budget = std::min<size_t>(budget, (size_t)((double)(free_b - fixed) * 0.4));
     }
-    int64_t n1t = (int64_t)(budget / row_bytes);
-    n1t = std::max<int64_t>(1, std::min<int64_t>(n1t, n1));
-    if (R.tile_rows > 0)
-        n1t = std::min<int64_t>(n1t, R.tile_rows);
+    int64_t n1t, kb;
+    plan_rows(R, budget, &n1t, &kb);
     const int n_tiles = (int)((n1 + n1t - 1) / n1t);
     constexpr int kTileEv = 6;
     if (stats) {
@@ -565,8 +598,8 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     d_f2 = (double *)p;
     CUTC_TRY(W.get(S_G, 4 * (size_t)n1t * n2 * 8, &p));
     d_G = (double *)p;
-    CUTC_TRY(W.get(S_XP, 4 * (size_t)n1t * np * 8, &p));
-    d_Xt = (double *)p;
+    CUTC_TRY(W.get(S_XP, 4 * (size_t)kb * np * 8, &p));
+    d_Xt = (double *)p;  // the int_2e block: Xt[(m blk_rows + i) np + p]
     CUTC_TRY(W.get(S_H, (size_t)np * np * 8, &p));
     d_H = (double *)p;
     CUTC_TRY(W.get(S_N, (size_t)np * std::max<int64_t>(nl, 1) * 8, &p));
@@ -581,9 +614,9 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         }
     }
     if (R.precision == CUTC_PLAIN_FP64) {
-        CUTC_TRY(W.get(S_S0, (size_t)np * n1t * 8, &p));
+        CUTC_TRY(W.get(S_S0, (size_t)np * kb * 8, &p));
         d_S0 = (double *)p;
-        CUTC_TRY(W.get(S_SL, (size_t)std::max<int64_t>(nl, 1) * 3 * n1t * 8, &p));
+        CUTC_TRY(W.get(S_SL, (size_t)std::max<int64_t>(nl, 1) * 3 * kb * 8, &p));
         d_Sl = (double *)p;
     }
     CUTC_TRY(launch_r2_terms(st, n2, nN, d_r2, d_rn, R.a_en, d_f2));
@@ -684,9 +717,13 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         CUTC_TRY(W.get(S_BLASWS, blas_ws, &p));
         CUBLAS_TRY(cublasSetWorkspace(E->blas, p, blas_ws));
     }
+    int64_t blk0 = 0;                                  // first r1 row of the int_2e block
+    int blk_rows = (int)std::min<int64_t>(kb, n1);     // its rows (whole tiles)
+    bool first_blk = true;
     for (int tile = 0; tile < n_tiles; tile++) {
         const int i0 = (int)(tile * n1t);
         const int nb = (int)std::min<int64_t>(n1t, n1 - i0);
+        const int ib = (int)(i0 - blk0);  // the tile's first row within the block
         cudaEvent_t *tev = stats ? &E->tile_ev[kTileEv * tile] : nullptr;
         CUTC_TRY(launch_r1_terms(st, i0, nb, nN, d_r1, d_rn, R.a_en, d_t1));
         if (tev)
@@ -724,45 +761,54 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         if (tev)
             CUTC_CUDA_TRY(cudaEventRecord(tev[1], st));
 
-        // X rows of the tile: Xt[(m nb + i) np + p] = sum_g P[p n2 + g] G[m plane + i n2 + g]
+        // X rows of the tile into the block:
+        //   Xt[(m blk_rows + ib + i) np + p] = sum_g P[p n2 + g] G[m plane + i n2 + g]
         if (R.precision == CUTC_PLAIN_FP64) {
             const double one = 1.0, zero = 0.0;
             if (tev)
                 CUTC_CUDA_TRY(cudaEventRecord(tev[2], st));
             CUBLAS_TRY(cublasDgemmStridedBatched(
                 E->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)np, nb, n2, &one, d_P, n2, 0, d_G, n2,
-                (long long)nb * n2, &zero, d_Xt, (int)np, (long long)nb * np, 4));
+                (long long)nb * n2, &zero, d_Xt + (int64_t)ib * np, (int)np,
+                (long long)blk_rows * np, 4));
             if (tev)
                 CUTC_CUDA_TRY(cudaEventRecord(tev[3], st));
         } else {
             CUTC_TRY(split_x_tile(E, R, st, sp, reinterpret_cast<const float2 *>(d_G), nb, d_Xt,
-                                  tev ? tev[2] : nullptr, tev ? tev[3] : nullptr, !R.pair_fp64));
+                                  blk_rows, ib, tev ? tev[2] : nullptr, tev ? tev[3] : nullptr,
+                                  !R.pair_fp64));
         }
 
-        // the tile's share of int_2e (src/build_int_2e_ao.cu:60-67 and 97-104, packed):
-        //   H += X_3 S0,   N += -1/2 [X_0 X_1 X_2] S   over the tile's r1 points
+        // the block's share of int_2e once its last tile is in
+        // (src/build_int_2e_ao.cu:60-67 and 97-104, packed):
+        //   H += X_3 S0,   N += -1/2 [X_0 X_1 X_2] S   over the block's r1 points
         if (tev)
             CUTC_CUDA_TRY(cudaEventRecord(tev[4], st));
-        if (R.precision == CUTC_PLAIN_FP64) {
-            const bool keep = nb == n1 && R.mol_tag && E->tag_i == R.mol_tag && E->tag_i_buf == d_S0;
-            if (!keep) {
-                CUTC_TRY(launch_sym_products(st, nb, nA, d_wr1 + i0, d_aos1 + i0, n1, d_S0, nb));
-                CUTC_TRY(launch_antisym_products(st, nb, nA, d_wr1 + i0, d_aos1 + i0, n1, d_Sl,
-                                                 3 * (int64_t)nb));
-                note_launches(2);
+        if (i0 + nb == blk0 + blk_rows) {
+            const int K = blk_rows;
+            const double *w1 = d_wr1 + blk0, *a1 = d_aos1 + blk0;
+            if (R.precision == CUTC_PLAIN_FP64) {
+                const bool keep =
+                    K == n1 && R.mol_tag && E->tag_i == R.mol_tag && E->tag_i_buf == d_S0;
+                if (!keep) {
+                    CUTC_TRY(launch_sym_products(st, K, nA, w1, a1, n1, d_S0, K));
+                    CUTC_TRY(launch_antisym_products(st, K, nA, w1, a1, n1, d_Sl, 3 * (int64_t)K));
+                    note_launches(2);
+                }
+                E->tag_i = K == n1 ? R.mol_tag : 0;
+                E->tag_i_buf = d_S0;
+                const double one = 1.0, mhalf = -0.5, beta = first_blk ? 0.0 : 1.0;
+                CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)np, K,
+                                       &one, d_Xt + 3 * (int64_t)K * np, (int)np, d_S0, K, &beta,
+                                       d_H, (int)np));
+                if (nl > 0)
+                    CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)nl,
+                                           3 * K, &mhalf, d_Xt, (int)np, d_Sl, 3 * K, &beta, d_N,
+                                           (int)np));
+            } else {
+                CUTC_TRY(split_int2e_tile(E, R, st, sp, w1, a1, n1, K, d_Xt, d_H, d_N, first_blk));
             }
-            E->tag_i = nb == n1 ? R.mol_tag : 0;
-            E->tag_i_buf = d_S0;
-            const double one = 1.0, mhalf = -0.5, beta = tile == 0 ? 0.0 : 1.0;
-            CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)np, nb, &one,
-                                   d_Xt + 3 * (int64_t)nb * np, (int)np, d_S0, nb, &beta, d_H,
-                                   (int)np));
-            if (nl > 0)
-                CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)nl, 3 * nb,
-                                       &mhalf, d_Xt, (int)np, d_Sl, 3 * nb, &beta, d_N, (int)np));
-        } else {
-            CUTC_TRY(split_int2e_tile(E, R, st, sp, d_wr1 + i0, d_aos1 + i0, n1, nb, d_Xt, d_H,
-                                      d_N, tile == 0));
+            first_blk = false;
         }
         if (tev)
             CUTC_CUDA_TRY(cudaEventRecord(tev[5], st));
@@ -770,19 +816,25 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         // the tile's X rows in the reference layout X[m][i][b][a]
         if (out_dev) {
             for (int m = 0; m < R.x_components; m++)
-                CUTC_TRY(launch_expand_pairs(st, nb, nA, d_Xt + (int64_t)m * nb * np, np,
-                                             R.X + ((int64_t)m * n1 + i0) * nA2));
+                CUTC_TRY(launch_expand_pairs(st, nb, nA, d_Xt + ((int64_t)m * blk_rows + ib) * np,
+                                             np, R.X + ((int64_t)m * n1 + i0) * nA2));
         } else {
             const int b = tile & 1;
             if (busy[b])
                 CUTC_CUDA_TRY(cudaStreamWaitEvent(st, done[b], 0));
-            CUTC_TRY(launch_expand_pairs(st, (int64_t)R.x_components * nb, nA, d_Xt, np, stage_x[b]));
+            for (int m = 0; m < R.x_components; m++)
+                CUTC_TRY(launch_expand_pairs(st, nb, nA, d_Xt + ((int64_t)m * blk_rows + ib) * np,
+                                             np, stage_x[b] + (int64_t)m * nb * nA2));
             CUTC_CUDA_TRY(cudaEventRecord(ready[b], st));
             CUTC_TRY(copy_x(tile));
             if (tile > 0)
                 CUTC_TRY(finish_x(tile - 1));
         }
-        note_launches(out_dev ? R.x_components : 1);
+        note_launches(R.x_components);
+        if (i0 + nb == blk0 + blk_rows) {  // next block
+            blk0 += blk_rows;
+            blk_rows = (int)std::min<int64_t>(kb, n1 - blk0);
+        }
     }
     if (!out_dev && n_tiles > 0)
         CUTC_TRY(finish_x(n_tiles - 1));
@@ -981,6 +1033,8 @@ extern "C" int cutc_int_ex(const cutc_options *opt, int n_grid1, int n_grid2, in
     R.X = int2_grad1_u12_ao; R.I = int_2e_ao;
     const char *tr = getenv("CUTC_TILE_ROWS");
     R.tile_rows = tr ? atoi(tr) : 0;
+    const char *ir = getenv("CUTC_INT2E_ROWS");
+    R.int2e_rows = ir ? atoi(ir) : 0;
     if (stats)
         memset(stats, 0, sizeof(*stats));
     std::lock_guard<std::mutex> lk(E->mu);

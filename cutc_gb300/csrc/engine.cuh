@@ -67,7 +67,8 @@ struct Request {
     int in_device = 0;        // molecule arrays (r1 .. aos2) on the device
     int out_device = 0;       // X and int_2e on the device
     size_t max_work_bytes = 0;
-    int tile_rows = 0;  // optional cap on r1 rows per tile
+    int tile_rows = 0;  // optional cap on r1 rows per X tile
+    int int2e_rows = 0; // optional cap on r1 rows per int_2e block
     int pair_fp64 = 0;  // split form: FP64 pair terms
     int k_split = 0;    // split form: max K per tensor-core launch (0 = default)
     int int2e_layout = CUTC_INT2E_PQST;

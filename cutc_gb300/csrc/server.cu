@@ -337,7 +337,7 @@ extern "C" void cutc_server_default_config(cutc_server_config *cfg)
     cfg->n_slots = 4;
     cfg->device_budget_bytes = 0;      // 0: 3/4 of free memory at creation
     cfg->cache_budget_bytes = 0;       // 0: 1/4 of the device budget
-    cfg->tile_budget_bytes = (size_t)4 << 30;
+    cfg->tile_budget_bytes = (size_t)8 << 30;
 }
 
 extern "C" int cutc_server_create(const cutc_server_config *cfg_in, cutc_server **out)
@@ -364,7 +364,7 @@ extern "C" int cutc_server_create(const cutc_server_config *cfg_in, cutc_server 
     if (cfg.cache_budget_bytes == 0)
         cfg.cache_budget_bytes = cfg.device_budget_bytes / 4;
     if (cfg.tile_budget_bytes == 0)
-        cfg.tile_budget_bytes = (size_t)4 << 30;
+        cfg.tile_budget_bytes = (size_t)8 << 30;
     Server *S = new Server();
     S->device = E0->device;
     S->cfg = cfg;

@@ -721,13 +721,17 @@ enum SplitSlot {
 
 size_t split_r1_row_bytes(const Request &R)
 {
+    // slices of the four G rows of one r1 point
+    return 2 * (size_t)R.n_slices * 4 * (size_t)round_up(R.n2, kBK) + 64;
+}
+
+size_t split_int2e_row_bytes(const Request &R)
+{
     const int64_t np = n_pairs(R.nA), nl = std::max<int64_t>(1, n_strict_pairs(R.nA));
     const int bn = bn_for(R.n_slices);
-    const size_t S2 = 2 * (size_t)R.n_slices;
-    // slices of the four G rows of one r1 point, plus the point's K columns of the
-    // int_2e operands (X_3, X_012, S0, S)
-    return S2 * (4 * (size_t)round_up(R.n2, kBK) + round_up(np, kBM) * 4 + round_up(np, bn) +
-                 3 * (size_t)round_up(nl, bn)) + 64;
+    // the point's K columns of the int_2e operands (X_3, X_012, S0, S)
+    return 2 * (size_t)R.n_slices * (round_up(np, kBM) * 4 + round_up(np, bn) +
+                                     3 * (size_t)round_up(nl, bn)) + 64;
 }
 
 size_t split_fixed_bytes(const Request &R)
@@ -790,7 +794,8 @@ int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *
 }
 
 int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const float2 *G,
-                 int nb, double *Xt, cudaEvent_t gemm_begin, cudaEvent_t gemm_end, bool have_rmax)
+                 int nb, double *Xb, int blk_rows, int ib, cudaEvent_t gemm_begin,
+                 cudaEvent_t gemm_end, bool have_rmax)
 {
     (void)E;
     SplitPlan &S_ = sp;
@@ -803,7 +808,8 @@ int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, co
         CUTC_TRY((slice_rows<S, SrcDenseDF>(st, src, B, have_rmax)));
         if (gemm_begin)
             CUTC_CUDA_TRY(cudaEventRecord(gemm_begin, st));
-        CUTC_TRY((gemm<S>(st, S_.AX, B, 1.0, Xt, np, B.M, 0, 0, 0, S_.err, R.k_split)));
+        // column (c, i) of the tile -> column c blk_rows + ib + i of the block
+        CUTC_TRY((gemm<S>(st, S_.AX, B, 1.0, Xb, np, nb, blk_rows, ib, 0, S_.err, R.k_split)));
         if (gemm_end)
             CUTC_CUDA_TRY(cudaEventRecord(gemm_end, st));
     });

@@ -31,19 +31,24 @@ struct SplitPlan {
     int *err = nullptr;                // device flag set by a bounded wait that gave up
 };
 
-// Device bytes per r1 row of a tile (slices of G and of the tile's int_2e operands).
+// Device bytes per r1 row of an X tile (slices of G).
 size_t split_r1_row_bytes(const Request &R);
+// Device bytes per r1 row of an int_2e block (slices of its int_2e operands).
+size_t split_int2e_row_bytes(const Request &R);
 // Device bytes that do not depend on the tile size (the P slices).
 size_t split_fixed_bytes(const Request &R);
 int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *wr2,
                     const double *aos2v, int64_t n1t, int slot0, SplitPlan &sp);
-// X of one r1 tile: Xt[(m nb + i) np + p] from the df tile G[c][i][j] ((hi, lo) pairs).
-// have_rmax: the row maxima of G are already in sp.BX.rmax (rows c nb + i)
+// X of one r1 tile from the df tile G[c][i][j] ((hi, lo) pairs), written into the
+// int_2e block buffer Xb[(m blk_rows + ib + i) np + p] (the tile starts at row ib of
+// a block of blk_rows rows).  have_rmax: the row maxima of G are already in
+// sp.BX.rmax (rows c nb + i).
 int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, const float2 *G,
-                 int nb, double *Xt, cudaEvent_t gemm_begin, cudaEvent_t gemm_end,
-                 bool have_rmax = false);
-// Adds the r1 tile's share of the int_2e contractions to H and N (overwrites when
-// first): wr1 and aos1 point at the tile's first row, ld1 is the row stride of aos1.
+                 int nb, double *Xb, int blk_rows, int ib, cudaEvent_t gemm_begin,
+                 cudaEvent_t gemm_end, bool have_rmax = false);
+// Adds an r1 block's share of the int_2e contractions to H and N (overwrites when
+// first): wr1 and aos1 point at the block's first row, ld1 is the row stride of aos1,
+// Xt[(m nb + i) np + p] holds the block's X rows.
 int split_int2e_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
                      const double *wr1, const double *aos1, int64_t ld1, int nb, const double *Xt,
                      double *H, double *N, bool first);

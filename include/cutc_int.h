@@ -216,7 +216,8 @@ typedef struct cutc_server_config {
     int n_slots;                /* concurrent requests on the GPU (default 4) */
     size_t device_budget_bytes; /* admission budget for requests in flight (0: 3/4 of free) */
     size_t cache_budget_bytes;  /* molecule cache (0: 1/4 of the device budget) */
-    size_t tile_budget_bytes;   /* r1-tile working set per request (default 4 GiB) */
+    size_t tile_budget_bytes;   /* per request: X-tile and int_2e-block working sets, each
+                                   (default 8 GiB) */
 } cutc_server_config;
 
 typedef struct cutc_request {

@@ -116,3 +116,33 @@ def test_pinned_outputs_match_pageable(tile_rows):
     assert s == 0, cg.last_error()
     assert np.array_equal(Xp.numpy(), Xh)
     assert np.array_equal(Ip.numpy(), Ih)
+
+
+@pytest.fixture
+def int2e_rows():
+    """Caps the r1 rows per int_2e block (rounded down to whole X tiles)."""
+    old = os.environ.get("CUTC_INT2E_ROWS")
+    set_ = _env_setter("CUTC_INT2E_ROWS")
+    yield set_
+    set_(old)
+
+
+@pytest.mark.parametrize("prec", [cg.PLAIN_FP64, cg.SPLIT_BF16])
+def test_int2e_blocks_span_tiles(prec, tile_rows, int2e_rows):
+    """X tiles of 40 rows feed int_2e blocks of 120 rows (517 = 4 x 120 + 37: a ragged
+    last block of a ragged last tile); X is the same bits as one tile and int_2e
+    differs by the block sum order (and, split form, the per-block slice scales)."""
+    p = _problem()
+    X1, I1 = cg.build_integrals(p, prec)
+    tile_rows(40)
+    int2e_rows(120)
+    X2, I2, st = cg.build_integrals(p, prec, with_stats=True)
+    assert st["n_r1_tiles"] == 13
+    if prec == cg.SPLIT_BF16:
+        assert np.array_equal(X2, X1)
+    else:
+        assert oracle.rel_err(X2, X1)["max"] < 1e-14
+    assert oracle.rel_err(I2, I1)["max"] < (1e-13 if prec == cg.PLAIN_FP64 else 1e-12)
+    Xo, Io = oracle.cutc_int(p)
+    ex, ei = oracle.rel_err(X2, Xo), oracle.rel_err(I2, Io)
+    assert ex["max"] < TOL[prec] and ei["max"] < TOL[prec], (ex, ei)
