@@ -33,10 +33,20 @@ EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_int_scan", "cutc_default_options", "
            "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_validate_launch_dims",
            "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
            "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy",
-           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos", "cutc_x_ao_to_mo"]
+           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos", "cutc_x_ao_to_mo", "cutc_plan"]
 
 INT2E_PQST = 0
 INT2E_PSQT = 1
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int) for k in ("tile_rows", "block_rows", "n_tiles", "n_blocks",
+                                            "slab_cols")] + \
+               [(k, ctypes.c_size_t) for k in ("budget_bytes", "fixed_bytes", "tile_row_bytes",
+                                               "block_row_bytes", "footprint_bytes")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Basis(ctypes.Structure):
@@ -153,6 +163,8 @@ def load(path: str = LIB_PATH):
     L.cutc_eval_aos.restype = i
     L.cutc_x_ao_to_mo.argtypes = [i, i, i, i, vp, vp, vp, vp, i, vp]
     L.cutc_x_ao_to_mo.restype = i
+    L.cutc_plan.argtypes = [ctypes.POINTER(Options), i, i, i, i, ctypes.POINTER(PlanInfo)]
+    L.cutc_plan.restype = i
     L.cutc_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
     L.cutc_server_default_config.restype = None
     L.cutc_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
@@ -285,6 +297,17 @@ def scan_integrals(p, c_sets, a_en=None, a_ee=None, precision=PLAIN_FP64, n_slic
     if s != CUTC_OK:
         raise CutcError(s, last_error())
     return (X, I, st.as_dict()) if with_stats else (X, I)
+
+
+def plan(n_grid1, n_grid2, n_ao, n_nuc, precision=PLAIN_FP64, n_slices=None, x_components=3,
+         device_pointers=False, max_work_bytes=0) -> dict:
+    """The device-memory plan of a build (cutc_plan): tiles, blocks and bytes."""
+    opt = options(precision, n_slices, 1.0, 1.0, x_components, device_pointers, max_work_bytes)
+    info = PlanInfo()
+    s = load().cutc_plan(ctypes.byref(opt), n_grid1, n_grid2, n_ao, n_nuc, ctypes.byref(info))
+    if s != CUTC_OK:
+        raise CutcError(s, last_error())
+    return info.as_dict()
 
 
 def eval_aos(shells, r, components=4):

@@ -1254,3 +1254,58 @@ extern "C" int cutc_eval_aos(const cutc_basis *basis, int n_points, const double
     CUTC_CUDA_TRY(cudaStreamSynchronize(st));
     return CUTC_OK;
 }
+
+extern "C" int cutc_plan(const cutc_options *opt, int n_grid1, int n_grid2, int n_ao, int n_nuc,
+                         cutc_plan_info *plan)
+{
+    using namespace cutc;
+    cutc_options defaults;
+    if (!opt) {
+        cutc_default_options(&defaults);
+        opt = &defaults;
+    }
+    if (!plan || n_grid1 <= 0 || n_grid2 <= 0 || n_ao <= 0 || n_nuc <= 0 ||
+        (opt->precision == CUTC_SPLIT_BF16 && (opt->n_slices < 3 || opt->n_slices > kMaxSlices)) ||
+        (opt->x_components != 3 && opt->x_components != 4)) {
+        cutc_set_error(CUTC_ERR_INVALID, "invalid plan arguments");
+        return CUTC_ERR_INVALID;
+    }
+    Request R{};
+    R.precision = opt->precision;
+    R.n_slices = opt->n_slices;
+    R.x_components = opt->x_components;
+    R.device_pointers = opt->device_pointers;
+    R.n1 = n_grid1; R.n2 = n_grid2; R.nA = n_ao; R.nN = n_nuc;
+    if (const char *tr = getenv("CUTC_TILE_ROWS"))
+        R.tile_rows = atoi(tr);
+    if (const char *ir = getenv("CUTC_INT2E_ROWS"))
+        R.int2e_rows = atoi(ir);
+    size_t budget = opt->max_work_bytes;
+    if (budget == 0) {
+        size_t free_b = 0, total_b = 0;
+        cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cutc_set_error(CUTC_ERR_NO_DEVICE, "no device to size the default budget: %s",
+                           cudaGetErrorString(e));
+            return CUTC_ERR_NO_DEVICE;
+        }
+        budget = std::min<size_t>((size_t)24 << 30, free_b / 4);
+        const size_t fixed = fixed_bytes(R);
+        if (free_b > fixed)
+            budget = std::min<size_t>(budget, (size_t)((double)(free_b - fixed) * 0.4));
+    }
+    int64_t n1t, kb;
+    plan_rows(R, budget, &n1t, &kb);
+    plan->tile_rows = (int)n1t;
+    plan->block_rows = (int)kb;
+    plan->n_tiles = (int)((n_grid1 + n1t - 1) / n1t);
+    plan->n_blocks = (int)((n_grid1 + kb - 1) / kb);
+    plan->slab_cols = int2e_slab_cols(n_ao);
+    plan->budget_bytes = budget;
+    plan->fixed_bytes = fixed_bytes(R);
+    plan->tile_row_bytes = r1_row_bytes(R);
+    plan->block_row_bytes = int2e_row_bytes(R);
+    plan->footprint_bytes = build_footprint(R, budget);
+    return CUTC_OK;
+}

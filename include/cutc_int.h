@@ -247,6 +247,25 @@ int cutc_server_get_stats(cutc_server *server, cutc_server_stats *stats);
 /* Finishes the queued requests, then frees the contexts and the cache. */
 void cutc_server_destroy(cutc_server *server);
 
+/* The device-memory plan of a build, computed on the host (no GPU needed when
+ * opt->max_work_bytes is set; with 0 the budget follows the current device's
+ * free memory, as a build would).  The r1 grid is cut into X tiles of
+ * tile_rows points; the int_2e contractions run once per block of block_rows
+ * points (whole tiles).  Device bytes besides the caller's arrays: fixed_bytes
+ * + tile_rows * tile_row_bytes + block_rows * block_row_bytes (+ the molecule
+ * arrays for host inputs) = footprint_bytes, which the server admits by.
+ * Honours CUTC_TILE_ROWS / CUTC_INT2E_ROWS like cutc_int_ex.  No reference
+ * counterpart. */
+typedef struct cutc_plan_info {
+    int tile_rows, block_rows, n_tiles, n_blocks;
+    int slab_cols;              /* int_2e columns per output slab (host outputs) */
+    size_t budget_bytes;        /* the budget each of tile and block was sized to */
+    size_t fixed_bytes, tile_row_bytes, block_row_bytes, footprint_bytes;
+} cutc_plan_info;
+
+int cutc_plan(const cutc_options *opt, int n_grid1, int n_grid2, int n_ao, int n_nuc,
+              cutc_plan_info *plan);
+
 /* AO values (components = 1) or values and gradients (components = 4) of the
  * basis at n_points points r(3, n_points), written as aos(n_points, n_ao,
  * components) column-major: the layout of aos_data1 / aos_data2.  r and aos are

@@ -61,3 +61,41 @@ def test_memory_admission_serialises_when_only_one_fits():
     for (X, I, _), (p, key, prec) in zip(outs, reqs):
         Xa, Ia = cg.build_integrals(p, prec)
         assert np.array_equal(X, Xa) and np.array_equal(I, Ia)
+
+
+def test_failed_request_is_isolated():
+    """A request that fails validation (a Jastrow exponent of 7) reports its status
+    through wait(); the requests around it complete with their standalone results."""
+    reqs = _mix()[:4]
+    bad = dataclasses.replace(reqs[1][0], m_bh=reqs[1][0].m_bh.copy())
+    bad.m_bh[0, 0] = 7
+    with cg.Server(n_slots=2) as srv:
+        tickets = [srv.submit(p, key, prec) for p, key, prec in reqs[:2]]
+        tb = srv.submit(bad, 0, cg.PLAIN_FP64)
+        tickets += [srv.submit(p, key, prec) for p, key, prec in reqs[2:]]
+        with pytest.raises(cg.CutcError) as e:
+            srv.wait(tb)
+        assert e.value.status == cg.CUTC_ERR_INVALID
+        for (p, key, prec), t in zip(reqs, tickets):
+            X, I, _ = srv.wait(t)
+            Xs, Is = cg.build_integrals(p, prec)
+            assert np.array_equal(X, Xs) and np.array_equal(I, Is)
+        st = srv.stats()
+    assert st["failed"] == 1 and st["completed"] == len(reqs)
+
+
+def test_cache_evicts_within_its_budget():
+    """A cache budget that holds one molecule: repeats of the most recent molecule
+    hit, a new molecule evicts the old one, and every result is still right."""
+    a = synth.make_problem(n_nuc=2, n_ao=6, n_grid1=200, n_grid2=800, size_bh=5, seed=51)
+    b = synth.make_problem(n_nuc=2, n_ao=7, n_grid1=220, n_grid2=900, size_bh=5, seed=52)
+    one = 8 * (4 * 220 + 4 * 900 + 6 + 4 * 220 * 7 + 900 * 7) + 4096
+    with cg.Server(n_slots=1, cache_budget_bytes=one) as srv:
+        order = [(a, 1), (a, 1), (b, 2), (a, 1)]
+        for p, key in order:
+            X, I, _ = srv.wait(srv.submit(p, key, cg.SPLIT_BF16))
+            Xs, Is = cg.build_integrals(p, cg.SPLIT_BF16)
+            assert np.array_equal(X, Xs) and np.array_equal(I, Is)
+        st = srv.stats()
+    assert st["cache_hits"] == 1 and st["cache_misses"] == 3
+    assert st["cache_bytes"] <= one
