@@ -1221,6 +1221,7 @@ extern "C" void cutc_release(void)
     cudaStreamSynchronize(E->xfer);
     E->ws.release();
     E->pinned.release();
+    E->tag_x = E->tag_i = 0;  // the operands they name are gone
 }
 
 extern "C" int cutc_eval_aos(const cutc_basis *basis, int n_points, const double *r,

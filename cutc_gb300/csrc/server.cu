@@ -319,8 +319,10 @@ static void worker(Server *S, int slot)
             }
             S->t_last_end = job->t_end;
             // an idle context keeps no memory while others wait for it
-            if (!S->queue.empty() && S->reserved + S->queue.front()->footprint > S->cfg.device_budget_bytes)
+            if (!S->queue.empty() && S->reserved + S->queue.front()->footprint > S->cfg.device_budget_bytes) {
                 E->ws.release();
+                E->tag_x = E->tag_i = 0;
+            }
         }
         S->cv_done.notify_all();
         S->cv_work.notify_all();
