@@ -304,12 +304,12 @@ static void worker(Server *S, int slot)
             cudaStreamSynchronize(E->stream);
         if (m)
             release_molecule(S, m);
+        bool release = false;
+        const size_t footprint = job->footprint;
         {
             std::lock_guard<std::mutex> lk(S->mu);
             job->t_end = Clock::now();
-            job->status = status;
-            S->reserved -= job->footprint;
-            S->in_flight--;
+            job->status = status;  // job may be freed by its waiter from here on
             if (status == CUTC_OK) {
                 S->completed++;
                 S->latencies_ms.push_back(
@@ -319,10 +319,20 @@ static void worker(Server *S, int slot)
             }
             S->t_last_end = job->t_end;
             // an idle context keeps no memory while others wait for it
-            if (!S->queue.empty() && S->reserved + S->queue.front()->footprint > S->cfg.device_budget_bytes) {
-                E->ws.release();
-                E->tag_x = E->tag_i = 0;
-            }
+            release = !S->queue.empty() &&
+                      S->reserved - footprint + S->queue.front()->footprint > S->cfg.device_budget_bytes;
+        }
+        S->cv_done.notify_all();  // the result is ready
+        if (release) {
+            // cudaFree waits for the whole device: done outside the lock, while this
+            // request's reservation still covers the memory being freed
+            E->ws.release();
+            E->tag_x = E->tag_i = 0;
+        }
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->reserved -= footprint;
+            S->in_flight--;
         }
         S->cv_done.notify_all();
         S->cv_work.notify_all();
