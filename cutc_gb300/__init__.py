@@ -33,7 +33,7 @@ EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_int_scan", "cutc_default_options", "
            "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_validate_launch_dims",
            "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
            "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy",
-           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos", "cutc_x_ao_to_mo", "cutc_plan"]
+           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos", "cutc_x_ao_to_mo", "cutc_plan", "cutc_pin_host", "cutc_unpin_host"]
 
 INT2E_PQST = 0
 INT2E_PSQT = 1
@@ -165,6 +165,10 @@ def load(path: str = LIB_PATH):
     L.cutc_x_ao_to_mo.restype = i
     L.cutc_plan.argtypes = [ctypes.POINTER(Options), i, i, i, i, ctypes.POINTER(PlanInfo)]
     L.cutc_plan.restype = i
+    L.cutc_pin_host.argtypes = [vp, ctypes.c_size_t]
+    L.cutc_pin_host.restype = i
+    L.cutc_unpin_host.argtypes = [vp]
+    L.cutc_unpin_host.restype = i
     L.cutc_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
     L.cutc_server_default_config.restype = None
     L.cutc_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
@@ -299,6 +303,22 @@ def scan_integrals(p, c_sets, a_en=None, a_ee=None, precision=PLAIN_FP64, n_slic
     return (X, I, st.as_dict()) if with_stats else (X, I)
 
 
+class PinnedArray:
+    """A host float64/uint8 numpy buffer page-locked with cutc_pin_host until close()."""
+
+    def __init__(self, nbytes):
+        self.array = np.empty(nbytes, dtype=np.uint8)
+        s = load().cutc_pin_host(_vp(self.array), nbytes)
+        if s != CUTC_OK:
+            raise CutcError(s, last_error())
+        self.nbytes = nbytes
+
+    def close(self):
+        if self.array is not None:
+            load().cutc_unpin_host(_vp(self.array))
+            self.array = None
+
+
 def plan(n_grid1, n_grid2, n_ao, n_nuc, precision=PLAIN_FP64, n_slices=None, x_components=3,
          device_pointers=False, max_work_bytes=0) -> dict:
     """The device-memory plan of a build (cutc_plan): tiles, blocks and bytes."""
@@ -410,10 +430,18 @@ class Server:
         self._live = {}
 
     def submit(self, p, molecule_key=0, precision=PLAIN_FP64, n_slices=None, x_components=3,
-               aos_from_basis=False):
-        """aos_from_basis: send p.shells instead of the AO arrays (evaluated on the GPU)."""
-        X = np.empty((x_components, p.n_grid1, p.n_ao ** 2))
-        I = np.empty((p.n_ao ** 2, p.n_ao ** 2))
+               aos_from_basis=False, out=None):
+        """aos_from_basis: send p.shells instead of the AO arrays (evaluated on the GPU).
+        out=(X, I): C-contiguous float64 arrays of shapes (x_components, n1, nA^2) and
+        (nA^2, nA^2) to fill (pinned memory is copied into directly)."""
+        if out is None:
+            X = np.empty((x_components, p.n_grid1, p.n_ao ** 2))
+            I = np.empty((p.n_ao ** 2, p.n_ao ** 2))
+        else:
+            X, I = out
+            assert X.shape == (x_components, p.n_grid1, p.n_ao ** 2) and X.dtype == np.float64
+            assert I.shape == (p.n_ao ** 2, p.n_ao ** 2) and I.dtype == np.float64
+            assert X.flags.c_contiguous and I.flags.c_contiguous
         arrs = dict(p.arrays())
         basis = make_basis(p.shells) if aos_from_basis else None
         if aos_from_basis:

@@ -1310,3 +1310,23 @@ extern "C" int cutc_plan(const cutc_options *opt, int n_grid1, int n_grid2, int 
     plan->footprint_bytes = build_footprint(R, budget);
     return CUTC_OK;
 }
+
+extern "C" int cutc_pin_host(void *ptr, size_t bytes)
+{
+    if (!ptr || bytes == 0) {
+        cutc_set_error(CUTC_ERR_INVALID, "nothing to pin");
+        return CUTC_ERR_INVALID;
+    }
+    CUTC_CUDA_TRY(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+    return CUTC_OK;
+}
+
+extern "C" int cutc_unpin_host(void *ptr)
+{
+    if (!ptr) {
+        cutc_set_error(CUTC_ERR_INVALID, "nothing to unpin");
+        return CUTC_ERR_INVALID;
+    }
+    CUTC_CUDA_TRY(cudaHostUnregister(ptr));
+    return CUTC_OK;
+}

@@ -247,6 +247,12 @@ int cutc_server_get_stats(cutc_server *server, cutc_server_stats *stats);
 /* Finishes the queued requests, then frees the contexts and the cache. */
 void cutc_server_destroy(cutc_server *server);
 
+/* Page-locks (pins) / releases caller host memory, so that outputs written there
+ * are copied in directly instead of through the library's pinned staging
+ * (cudaHostRegister / cudaHostUnregister).  No reference counterpart. */
+int cutc_pin_host(void *ptr, size_t bytes);
+int cutc_unpin_host(void *ptr);
+
 /* The device-memory plan of a build, computed on the host (no GPU needed when
  * opt->max_work_bytes is set; with 0 the budget follows the current device's
  * free memory, as a build would).  The r1 grid is cut into X tiles of

@@ -146,3 +146,24 @@ def test_int2e_blocks_span_tiles(prec, tile_rows, int2e_rows):
     Xo, Io = oracle.cutc_int(p)
     ex, ei = oracle.rel_err(X2, Xo), oracle.rel_err(I2, Io)
     assert ex["max"] < TOL[prec] and ei["max"] < TOL[prec], (ex, ei)
+
+
+def test_registered_outputs_match_pageable(tile_rows):
+    """Caller memory page-locked with cutc_pin_host takes the direct copy path."""
+    p = _problem()
+    tile_rows(40)
+    Xh, Ih = cg.build_integrals(p, cg.SPLIT_BF16)
+    nX, nI = 3 * p.n_grid1 * p.n_ao ** 2, p.n_ao ** 4
+    blk = cg.PinnedArray(8 * (nX + nI))
+    try:
+        a = blk.array.view(np.float64)
+        X = a[:nX].reshape(3, p.n_grid1, p.n_ao ** 2)
+        I = a[nX:].reshape(p.n_ao ** 2, p.n_ao ** 2)
+        opt = cg.options(cg.SPLIT_BF16, None, p.a_en, p.a_ee, 3, False, 0, None)
+        s = cg.cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                           p.r1, p.wr1, p.r2, p.wr2, p.rn, p.aos1, p.aos2,
+                           p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I)
+        assert s == 0, cg.last_error()
+        assert np.array_equal(X, Xh) and np.array_equal(I, Ih)
+    finally:
+        blk.close()
