@@ -133,8 +133,12 @@ void PinnedPool::release()
 // the copy itself both scale with threads).
 static void host_copy(void *dst, const void *src, size_t bytes)
 {
+    // first-touch page faults of fresh caller memory dominate large copies and
+    // scale with threads: up to half the host's cores
     const size_t kChunk = (size_t)16 << 20;
-    const int n = (int)std::min<size_t>(4, bytes / kChunk);
+    static const int kMaxThreads =
+        (int)std::max(2u, std::min(8u, std::thread::hardware_concurrency() / 2));
+    const int n = (int)std::min<size_t>(kMaxThreads, bytes / kChunk);
     if (n <= 1) {
         memcpy(dst, src, bytes);
         return;
