@@ -669,6 +669,9 @@ def run_serving(args):
         elapsed = time.perf_counter() - t0
         st = srv.stats()
     flops = sum(p.flops() for _, p in reqs)
+    accuracy = None
+    if not args.skip_accuracy:
+        accuracy = serving_accuracy(cg, reqs, args.slices)
     line = {"metric": "TC integral builds/s and latency, serving stream", "value": len(reqs) / elapsed,
             "unit": "builds/s", "n_gpus": 1, "higher_is_better": True,
             "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
@@ -681,9 +684,34 @@ def run_serving(args):
                        "host_output_budget_gb": args.host_gb},
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "arrivals_held_back_s": t_blocked,
-            "server": st, "alg_tflops": flops / elapsed / 1e12}
+            "server": st, "alg_tflops": flops / elapsed / 1e12, "accuracy": accuracy}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def serving_accuracy(cg, reqs, n_slices, rows=128, max_ao=200):
+    """Split vs plain FP64 for three molecules of the stream (smallest, median and
+    largest n_ao up to max_ao, so that int_2e stays a few GB), on `rows` r1 points
+    spread over each grid, AOs from the basis as in the stream."""
+    import dataclasses
+    from oracle.oracle import rel_err
+    mols = {}
+    for key, p in reqs:
+        if p.n_ao <= max_ao and key not in mols:
+            mols[key] = p
+    ps = sorted(mols.values(), key=lambda q: q.n_ao)
+    pick = [ps[0], ps[len(ps) // 2], ps[-1]] if len(ps) >= 3 else ps
+    out = []
+    for p in pick:
+        idx = np.unique(np.linspace(0, p.n_grid1 - 1, min(rows, p.n_grid1)).round().astype(np.int64))
+        sub = dataclasses.replace(p, r1=np.ascontiguousarray(p.r1[idx]),
+                                  wr1=np.ascontiguousarray(p.wr1[idx]))
+        Xs, Is = cg.build_integrals(sub, cg.SPLIT_BF16, n_slices=n_slices, aos_from_basis=True)
+        Xp, Ip = cg.build_integrals(sub, cg.PLAIN_FP64, aos_from_basis=True)
+        out.append({"n_nuc": p.n_nuc, "n_ao": p.n_ao, "n_grid2": p.n_grid2, "r1_rows": len(idx),
+                    "X_vs_fp64": rel_err(Xs, Xp), "int2e_vs_fp64": rel_err(Is, Ip)})
+        del Xs, Is, Xp, Ip
+    return out
 
 
 def run_scan(args):
