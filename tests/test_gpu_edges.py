@@ -1,0 +1,52 @@
+"""Edge cases of the sizes against the oracle, both forms: one AO (no strict pairs,
+so no antisymmetric part), two AOs, no Jastrow terms (everything exactly zero,
+including the split slicer's all-zero rows), single-point grids, and exponents at
+their upper limit of 6."""
+import numpy as np
+import pytest
+
+import cutc_gb300 as cg
+from cutc_gb300 import synth
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = {cg.PLAIN_FP64: 1e-12, cg.SPLIT_BF16: 1e-10}
+CASES = {
+    "one_ao": dict(n_nuc=1, n_ao=1, n_grid1=50, n_grid2=70, size_bh=3, seed=1),
+    "two_ao": dict(n_nuc=1, n_ao=2, n_grid1=40, n_grid2=60, size_bh=3, seed=2),
+    "single_points": dict(n_nuc=1, n_ao=3, n_grid1=1, n_grid2=1, size_bh=2, seed=4),
+    "one_r1_point": dict(n_nuc=2, n_ao=6, n_grid1=1, n_grid2=500, size_bh=4, seed=5),
+}
+
+
+def _check(X, I, Xo, Io, prec):
+    ex, ei = oracle.rel_err(X, Xo), oracle.rel_err(I, Io)
+    assert ex["max"] < TOL[prec] and ei["max"] < TOL[prec], (ex, ei)
+
+
+@pytest.mark.parametrize("prec", [cg.PLAIN_FP64, cg.SPLIT_BF16])
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_small_sizes(name, prec):
+    p = synth.make_problem(**CASES[name])
+    X, I = cg.build_integrals(p, prec)
+    assert np.all(np.isfinite(X)) and np.all(np.isfinite(I))
+    _check(X, I, *oracle.cutc_int(p), prec)
+
+
+@pytest.mark.parametrize("prec", [cg.PLAIN_FP64, cg.SPLIT_BF16])
+def test_no_jastrow_terms_gives_zeros(prec):
+    p = synth.make_problem(n_nuc=2, n_ao=5, n_grid1=30, n_grid2=40, size_bh=0, seed=3)
+    X, I = cg.build_integrals(p, prec)
+    assert not np.any(X) and not np.any(I)
+
+
+@pytest.mark.parametrize("prec", [cg.PLAIN_FP64, cg.SPLIT_BF16])
+def test_highest_exponents(prec):
+    """Exponents 5 and 6 (the reference's powd_int limit) and 1 in every slot."""
+    p = synth.make_problem(n_nuc=2, n_ao=6, n_grid1=120, n_grid2=400, size_bh=4, seed=6)
+    p.m_bh = np.ascontiguousarray(np.array([[6, 5, 1, 0], [0, 6, 2, 1]], dtype=np.int32))
+    p.n_bh = np.ascontiguousarray(np.array([[1, 6, 5, 2], [6, 0, 1, 5]], dtype=np.int32))
+    p.o_bh = np.ascontiguousarray(np.array([[5, 1, 6, 3], [1, 6, 0, 6]], dtype=np.int32))
+    X, I = cg.build_integrals(p, prec)
+    _check(X, I, *oracle.cutc_int(p), prec)
