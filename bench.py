@@ -35,7 +35,8 @@ from cutc_gb300 import synth  # noqa: E402
 
 METRIC = "TC integral builds/s (split-precision vs FP64 at 1e-10 rel err)"
 UNIT = "builds/s"
-CPU_SAMPLE_ROWS = 48
+CPU_SAMPLE_ROWS = 48        # per step of --impl reference
+CPU_BASELINE_ROWS = 256     # the cpu_baseline leg: about 10 s of oracle work on 16 cores
 
 
 def log(msg):
@@ -338,19 +339,23 @@ def run_ours(args):
     opt_h = cg.options(prec, args.slices, p.a_en, p.a_ee, 3, False, 0, stream.cuda_stream,
                        k_split=args.k_split)
 
-    def build_host():
+    def build_host(stats=None):
         s = cg.cutc_int_ex(opt_h, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
                            hp["r1"], hp["wr1"], hp["r2"], hp["wr2"], hp["rn"], hp["aos1"], hp["aos2"],
-                           hp["c_bh"], hp["m_bh"], hp["n_bh"], hp["o_bh"], Xh, Ih, None)
+                           hp["c_bh"], hp["m_bh"], hp["n_bh"], hp["o_bh"], Xh, Ih, stats)
         if s != cg.CUTC_OK:
             raise cg.CutcError(s, cg.last_error())
 
     build_host()
     barrier()
     e2e_steps = max(1, min(args.steps, 3))
+    e2e_phases = {}
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        build_host()
+        st = cg.Stats()
+        build_host(st)
+        for k, v in st.as_dict().items():
+            e2e_phases[k] = e2e_phases.get(k, 0) + v / e2e_steps
     barrier()
     e2e_s = time.perf_counter() - t0
     te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
@@ -397,7 +402,8 @@ def run_ours(args):
                "roofline": roofline,
                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
-                       "buffers": "pinned host memory through cutc_int_ex"},
+                       "buffers": "pinned host memory through cutc_int_ex",
+                       "phases_ms_per_step": e2e_phases},
                "phases_ms_per_step": {"pair": pair_ms / args.steps,
                                       "x_gemm": gemm_ms / args.steps}}
     # ---- accuracy and the plain FP64 rate on an r1 sample --------------------------
@@ -416,7 +422,7 @@ def run_ours(args):
         out["plain_fp64"] = plain_rate_estimate(cg, p, (rows, 2 * rows))
     if rank == 0 and world == 1 and not args.skip_cpu:
         log("cpu baseline sample")
-        cb, _, _ = cpu_sample(p)
+        cb, _, _ = cpu_sample(p, rows=min(CPU_BASELINE_ROWS, p.n_grid1))
         out["cpu_baseline"] = cb
     if rank == 0:
         print(json.dumps(out), flush=True)

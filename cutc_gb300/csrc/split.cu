@@ -19,7 +19,13 @@
 //     keeps the operand traffic under the shared-memory bandwidth;
 //   * every product of diagonal d is an integer multiple of 2^{-16-9d} of
 //     magnitude <= 2^{-9d}, so the FP32 accumulator holds the exact sum while
-//     (d + 1) * Kc * 2^16 <= 2^24; with the chunk Kc = 64 this holds for d <= 3;
+//     (d + 1) * Kc * 2^16 <= 2^24.  The chunk is Kc = 128: exact for d <= 1;
+//     diagonal 2 (3 * 128 * 2^16 = 1.5 * 2^24 quanta at most) can round only if
+//     a chunk sum of 384 remainder-digit products exceeds 2^24 quanta, and then
+//     by one quantum 2^-34, which over the whole K stays below 2^-41 of
+//     sum_k |a_k b_k| -- under the slicing's own representation error.  (Kc = 64
+//     keeps d = 2 provably exact but flushes twice as often: 9 % slower on the
+//     medium X contraction at the same measured error);
 //   * after each chunk the epilogue adds the d = 0, 1, 2 sums error-free into
 //     FP32 (hi, lo) register pairs (hi on a coarse grid, lo the remainder)
 //     and d >= 3 (relative size 2^-27) into a plain FP32 sum; nothing is
@@ -52,7 +58,7 @@ namespace cutc {
 
 constexpr int kBM = 128;        // rows of A per CTA (TMEM lanes)
 constexpr int kBK = 32;         // K per TMA box: 32 BF16 = 64-byte rows (64B swizzle)
-constexpr int kChunkBlocks = 2; // exact-accumulation chunk: 64 K
+constexpr int kChunkBlocks = 4; // exact-accumulation chunk: 128 K
 constexpr int kMaxKPerLaunch = 1 << 18;  // keeps every exact (hi, lo) sum below 2^24 units
 constexpr uint32_t kTmemCols = 512;
 constexpr int kGroupM = 8;      // row tiles per raster group (A tiles shared through L2)

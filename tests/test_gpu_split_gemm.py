@@ -7,9 +7,10 @@ product is bounded by
     |C - AB^T|_mn <= tol(S) * (max|A_m| |B_n|_1 + |A_m|_1 max|B_n|)
 
 with tol(S) = max(2^-(9S-3), 2^-50): the slice diagonals 0, 1 and 2 are
-accumulated exactly across the 64-wide K chunks, and the remaining diagonals
-(relative size 2^-27 and below) in FP32, so no error term grows with K beyond
-the FP64 recombination.
+accumulated exactly across the 128-wide K chunks (diagonal 2 can round only when
+its remainder digits add up coherently over a chunk, which random operands never
+do), and the remaining diagonals (relative size 2^-27 and below) in FP32, so no
+error term grows with K beyond the FP64 recombination.
 """
 import numpy as np
 import pytest
