@@ -33,10 +33,18 @@ EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_int_scan", "cutc_default_options", "
            "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_validate_launch_dims",
            "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
            "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy",
-           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos", "cutc_x_ao_to_mo", "cutc_plan", "cutc_pin_host", "cutc_unpin_host"]
+           "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos",
+           "cutc_x_ao_to_mo", "cutc_plan", "cutc_pin_host", "cutc_unpin_host",
+           "cutc_int_bh", "int_long_range", "int_short_range_herm", "int_short_range_nonherm",
+           "get_int2_grad1_u12_ao", "get_int_2e_ao"]
 
 INT2E_PQST = 0
 INT2E_PSQT = 1
+
+
+class Dim3(ctypes.Structure):
+    """CUDA's dim3 by value (cutc_dim3): the reference's launch-geometry argument."""
+    _fields_ = [("x", ctypes.c_uint), ("y", ctypes.c_uint), ("z", ctypes.c_uint)]
 
 
 class PlanInfo(ctypes.Structure):
@@ -159,6 +167,18 @@ def load(path: str = LIB_PATH):
     L.trans_pqst_psqt_inplace.restype = None
     L.trans_pqst_psqt_copy.argtypes = [i, vp, vp]
     L.trans_pqst_psqt_copy.restype = None
+    L.cutc_int_bh.argtypes = [Dim3, Dim3] + [i] * 8 + [vp] * 8
+    L.cutc_int_bh.restype = None
+    L.int_long_range.argtypes = [i] * 5 + [vp] * 3
+    L.int_long_range.restype = None
+    L.int_short_range_herm.argtypes = [i, i, vp, vp, vp]
+    L.int_short_range_herm.restype = None
+    L.int_short_range_nonherm.argtypes = [i, i, vp, vp, vp]
+    L.int_short_range_nonherm.restype = None
+    L.get_int2_grad1_u12_ao.argtypes = [Dim3, Dim3] + [i] * 5 + [vp] * 10
+    L.get_int2_grad1_u12_ao.restype = None
+    L.get_int_2e_ao.argtypes = [i, i] + [vp] * 4
+    L.get_int_2e_ao.restype = None
     L.cutc_eval_aos.argtypes = [ctypes.POINTER(Basis), i, vp, i, vp, i, vp]
     L.cutc_eval_aos.restype = i
     L.cutc_x_ao_to_mo.argtypes = [i, i, i, i, vp, vp, vp, vp, i, vp]

@@ -306,13 +306,14 @@ static int validate(const Request &R)
         cutc_set_error(CUTC_ERR_INVALID, "n_ao=%d too large", R.nA);
         return CUTC_ERR_INVALID;
     }
-    const void *ptrs[] = {R.r1, R.wr1, R.r2, R.wr2, R.rn, R.X, R.I};
+    const void *ptrs[] = {R.r1, R.r2, R.wr2, R.rn, R.X, R.x_only ? R.X : R.wr1,
+                          R.x_only ? R.X : R.I};
     for (const void *p : ptrs)
         if (!p) {
             cutc_set_error(CUTC_ERR_INVALID, "NULL array argument");
             return CUTC_ERR_INVALID;
         }
-    if (!R.aos1 || !R.aos2) {
+    if ((!R.aos1 && !R.x_only) || !R.aos2) {
         if (!R.basis) {
             cutc_set_error(CUTC_ERR_INVALID, "NULL AO array and no basis to evaluate it from");
             return CUTC_ERR_INVALID;
@@ -389,12 +390,14 @@ static size_t fixed_bytes(const Request &R)
 {
     const int64_t n2 = R.n2, nA = R.nA, nN = R.nN;
     const int64_t np = n_pairs(nA), nl = std::max<int64_t>(1, n_strict_pairs(nA));
-    double b = (double)nN * n2 * 8 + ((double)np * np + (double)np * nl) * 8;
+    double b = (double)nN * n2 * 8;
+    if (!R.x_only)
+        b += ((double)np * np + (double)np * nl) * 8;
     if (R.precision == CUTC_PLAIN_FP64)
         b += (double)np * n2 * 8;
     else
         b += (double)split_fixed_bytes(R) + (3.0 + nN) * n2 * sizeof(float2);
-    if (!(R.device_pointers || R.out_device))
+    if (!(R.device_pointers || R.out_device) && !R.x_only)
         b += 2.0 * int2e_slab_cols(R.nA) * nA * nA * 8;
     return (size_t)b;
 }
@@ -417,6 +420,8 @@ static size_t int2e_row_bytes(const Request &R)
 {
     const int64_t np = n_pairs(R.nA), nl = std::max<int64_t>(1, n_strict_pairs(R.nA));
     size_t b = 4 * (size_t)np * 8;
+    if (R.x_only)  // the packed X rows alone, staged for the expansion
+        return b;
     if (R.precision == CUTC_PLAIN_FP64)
         b += ((size_t)np + 3 * (size_t)nl) * 8;
     else
@@ -434,6 +439,11 @@ static void plan_rows(const Request &R, size_t budget, int64_t *n1t, int64_t *kb
     int64_t t = std::max<int64_t>(1, std::min<int64_t>((int64_t)(budget / r1_row_bytes(R)), n1));
     if (R.tile_rows > 0)
         t = std::min<int64_t>(t, R.tile_rows);
+    if (R.x_only) {  // no int_2e: the block is the tile
+        *n1t = t;
+        *kb = t;
+        return;
+    }
     int64_t k = std::max<int64_t>(1, std::min<int64_t>((int64_t)(budget / int2e_row_bytes(R)), n1));
     if (R.int2e_rows > 0)
         k = std::min<int64_t>(k, R.int2e_rows);
@@ -508,7 +518,8 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[0], st));
 
     // ---- inputs on the device --------------------------------------------
-    const double *d_r1, *d_wr1, *d_r2, *d_wr2, *d_rn, *d_aos1, *d_aos2v;
+    const double *d_r1 = nullptr, *d_wr1 = nullptr, *d_r2 = nullptr, *d_wr2 = nullptr;
+    const double *d_rn = nullptr, *d_aos1 = nullptr, *d_aos2v = nullptr;
     void *p;
     auto put = [&](int slot, const void *h, size_t bytes, const double **dst) -> int {
         CUTC_TRY(W.get(slot, bytes, &p));
@@ -524,7 +535,8 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         d_aos2v = R.aos2;  // component 0 is the first n2*nA block
     } else {
         CUTC_TRY(put(S_R1, R.r1, 3 * (size_t)n1 * 8, &d_r1));
-        CUTC_TRY(put(S_WR1, R.wr1, (size_t)n1 * 8, &d_wr1));
+        if (R.wr1)
+            CUTC_TRY(put(S_WR1, R.wr1, (size_t)n1 * 8, &d_wr1));
         CUTC_TRY(put(S_R2, R.r2, 3 * (size_t)n2 * 8, &d_r2));
         CUTC_TRY(put(S_WR2, R.wr2, (size_t)n2 * 8, &d_wr2));
         CUTC_TRY(put(S_RN, R.rn, 3 * (size_t)nN * 8, &d_rn));
@@ -534,11 +546,11 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         if (R.aos2)
             CUTC_TRY(put(S_AOS2, R.aos2, (size_t)n2 * nA * 8, &d_aos2v));
     }
-    if (!R.aos1 || !R.aos2) {
+    if ((!R.aos1 && !R.x_only) || !R.aos2) {
         // AO values (and r1 gradients) from the basis, on the device
         BasisDev B;
         CUTC_TRY(upload_basis(W, S_BASIS, st, R.basis, &B));
-        if (!R.aos1) {
+        if (!R.aos1 && !R.x_only) {
             CUTC_TRY(W.get(S_AOS1, 4 * (size_t)n1 * nA * 8, &p));
             CUTC_TRY(launch_eval_aos(st, B, n1, d_r1, 4, (double *)p, n1));
             d_aos1 = (const double *)p;
@@ -594,7 +606,8 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
 
     // ---- buffers -------------------------------------------------------------
     NucTerm *d_t1;
-    double *d_f2, *d_P = nullptr, *d_G, *d_Xt, *d_H, *d_N, *d_S0 = nullptr, *d_Sl = nullptr;
+    double *d_f2, *d_P = nullptr, *d_G, *d_Xt, *d_H = nullptr, *d_N = nullptr;
+    double *d_S0 = nullptr, *d_Sl = nullptr;
     double *stage_x[2] = {nullptr, nullptr}, *stage_i[2] = {nullptr, nullptr};
     CUTC_TRY(W.get(S_T1, (size_t)n1t * nN * sizeof(NucTerm), &p));
     d_t1 = (NucTerm *)p;
@@ -604,20 +617,24 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     d_G = (double *)p;
     CUTC_TRY(W.get(S_XP, 4 * (size_t)kb * np * 8, &p));
     d_Xt = (double *)p;  // the int_2e block: Xt[(m blk_rows + i) np + p]
-    CUTC_TRY(W.get(S_H, (size_t)np * np * 8, &p));
-    d_H = (double *)p;
-    CUTC_TRY(W.get(S_N, (size_t)np * std::max<int64_t>(nl, 1) * 8, &p));
-    d_N = (double *)p;
+    if (!R.x_only) {
+        CUTC_TRY(W.get(S_H, (size_t)np * np * 8, &p));
+        d_H = (double *)p;
+        CUTC_TRY(W.get(S_N, (size_t)np * std::max<int64_t>(nl, 1) * 8, &p));
+        d_N = (double *)p;
+    }
     const int slab = int2e_slab_cols(nA);
     if (!out_dev) {
         for (int k = 0; k < 2; k++) {
             CUTC_TRY(W.get(S_XOUT + k, (size_t)R.x_components * n1t * nA2 * 8, &p));
             stage_x[k] = (double *)p;
-            CUTC_TRY(W.get(S_IOUT + k, (size_t)slab * nA2 * 8, &p));
-            stage_i[k] = (double *)p;
+            if (!R.x_only) {
+                CUTC_TRY(W.get(S_IOUT + k, (size_t)slab * nA2 * 8, &p));
+                stage_i[k] = (double *)p;
+            }
         }
     }
-    if (R.precision == CUTC_PLAIN_FP64) {
+    if (R.precision == CUTC_PLAIN_FP64 && !R.x_only) {
         CUTC_TRY(W.get(S_S0, (size_t)np * kb * 8, &p));
         d_S0 = (double *)p;
         CUTC_TRY(W.get(S_SL, (size_t)std::max<int64_t>(nl, 1) * 3 * kb * 8, &p));
@@ -667,7 +684,7 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     cudaEvent_t ready[2] = {E->ev[3], E->ev[4]}, done[2] = {E->ev[9], E->ev[10]};
     bool busy[2] = {false, false};
     const bool x_direct = out_dev || async_host_ptr(R.X);
-    const bool i_direct = out_dev || async_host_ptr(R.I);
+    const bool i_direct = out_dev || R.x_only || async_host_ptr(R.I);
     double *hpin_x[2] = {nullptr, nullptr}, *hpin_i[2] = {nullptr, nullptr};
     for (int k = 0; k < 2 && !out_dev; k++) {
         if (!x_direct) {
@@ -788,7 +805,7 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         //   H += X_3 S0,   N += -1/2 [X_0 X_1 X_2] S   over the block's r1 points
         if (tev)
             CUTC_CUDA_TRY(cudaEventRecord(tev[4], st));
-        if (i0 + nb == blk0 + blk_rows) {
+        if (i0 + nb == blk0 + blk_rows && !R.x_only) {
             const int K = blk_rows;
             const double *w1 = d_wr1 + blk0, *a1 = d_aos1 + blk0;
             if (R.precision == CUTC_PLAIN_FP64) {
@@ -846,7 +863,9 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
 
     // ---- int_2e = A + A^T ------------------------------------------------------
     const bool psqt = R.int2e_layout == CUTC_INT2E_PSQT;
-    if (out_dev) {
+    if (R.x_only) {
+        // X alone: nothing to assemble
+    } else if (out_dev) {
         CUTC_TRY(launch_assemble_int2e(st, nA, d_H, d_N, 0, (int)nA2, psqt, R.I));
         note_launches(1);
     } else {
@@ -931,19 +950,22 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     return CUTC_OK;
 }
 
-int run_pair_only(Engine *E, int i0, int n1b, int n1, int n2, int nN, int nB, const double *r1,
-                  const double *r2, const double *rn, const double *c_bh, const int *m_bh,
-                  const int *n_bh, const int *o_bh, double a_en, double a_ee, double *G)
+// The pair terms alone, on device arrays: rows [i0, i0 + n1b) of r1 against the
+// r2 points [j0, j0 + n2b) of r2, into G[c * plane + i * ldg + j] (c = 0..3).
+int run_pair_only(Engine *E, cudaStream_t st, int i0, int n1b, int n1, int j0, int n2b,
+                  int64_t ldg, int64_t plane, int nN, int nB, const double *r1, const double *r2,
+                  const double *rn, const double *c_bh, const int *m_bh, const int *n_bh,
+                  const int *o_bh, double a_en, double a_ee, double *G)
 {
-    if (n1b <= 0 || n2 <= 0 || nN <= 0 || nB < 0 || i0 < 0 || i0 + n1b > n1 || nN > kMaxNuc ||
-        !r1 || !r2 || !rn || !G || !(a_en > 0) || !(a_ee > 0)) {
+    if (n1b <= 0 || n2b <= 0 || nN <= 0 || nB < 0 || i0 < 0 || j0 < 0 || i0 + n1b > n1 ||
+        nN > kMaxNuc || ldg < n2b || plane < (n1b - 1) * ldg + n2b || !r1 || !r2 || !rn || !G ||
+        !(a_en > 0) || !(a_ee > 0)) {
         cutc_set_error(CUTC_ERR_INVALID, "invalid pair-kernel arguments");
         return CUTC_ERR_INVALID;
     }
     // parameters come from the device: bring them to the host to build the term table
     std::vector<double> c((size_t)nN * nB);
     std::vector<int> m((size_t)nN * nB), n((size_t)nN * nB), o((size_t)nN * nB);
-    cudaStream_t st = E->stream;
     if (nB > 0) {
         CUTC_CUDA_TRY(cudaMemcpyAsync(c.data(), c_bh, c.size() * 8, cudaMemcpyDeviceToHost, st));
         CUTC_CUDA_TRY(cudaMemcpyAsync(m.data(), m_bh, m.size() * 4, cudaMemcpyDeviceToHost, st));
@@ -971,15 +993,16 @@ int run_pair_only(Engine *E, int i0, int n1b, int n1, int n2, int nN, int nB, co
     CUTC_CUDA_TRY(cudaMemcpyAsync(d_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice, st));
     CUTC_TRY(W.get(S_T1, (size_t)n1b * nN * sizeof(NucTerm), &p));
     NucTerm *d_t1 = (NucTerm *)p;
-    CUTC_TRY(W.get(S_F2, (size_t)nN * n2 * 8, &p));
+    CUTC_TRY(W.get(S_F2, (size_t)nN * n2b * 8, &p));
     double *d_f2 = (double *)p;
+    const double *r2w = r2 + 3 * (int64_t)j0;  // the r2 window
     CUTC_TRY(launch_r1_terms(st, i0, n1b, nN, r1, rn, a_en, d_t1));
-    CUTC_TRY(launch_r2_terms(st, n2, nN, r2, rn, a_en, d_f2));
+    CUTC_TRY(launch_r2_terms(st, n2b, nN, r2w, rn, a_en, d_f2));
     PairArgs P;
-    P.i0 = i0; P.n1b = n1b; P.n2 = n2; P.nN = nN; P.n_terms = (int)exps.size();
-    P.r1 = r1; P.r2 = r2; P.t1 = d_t1; P.f2 = d_f2;
+    P.i0 = i0; P.n1b = n1b; P.n2 = n2b; P.nN = nN; P.n_terms = (int)exps.size();
+    P.r1 = r1; P.r2 = r2w; P.t1 = d_t1; P.f2 = d_f2;
     P.coef = d_coef; P.exps = d_exps; P.term_off = d_off; P.a_ee = a_ee;
-    P.G = G; P.ldg = n2; P.plane = (int64_t)n1b * n2;
+    P.G = G; P.ldg = ldg; P.plane = plane;
     CUTC_TRY(launch_pair_f64(st, P));
     note_launches(3);
     CUTC_CUDA_TRY(cudaStreamSynchronize(st));
@@ -1035,6 +1058,7 @@ extern "C" int cutc_int_ex(const cutc_options *opt, int n_grid1, int n_grid2, in
     R.aos1 = aos_data1; R.aos2 = aos_data2;
     R.c_bh = c_bh; R.m_bh = m_bh; R.n_bh = n_bh; R.o_bh = o_bh;
     R.X = int2_grad1_u12_ao; R.I = int_2e_ao;
+    R.x_only = int_2e_ao == nullptr;
     const char *tr = getenv("CUTC_TILE_ROWS");
     R.tile_rows = tr ? atoi(tr) : 0;
     const char *ir = getenv("CUTC_INT2E_ROWS");
@@ -1178,8 +1202,9 @@ extern "C" int cutc_jast_bh_dev(int i0, int n1b, int n_grid1, int n_grid2, int n
     Engine *E = nullptr;
     CUTC_TRY(get_engine(&E));
     std::lock_guard<std::mutex> lk(E->mu);
-    return run_pair_only(E, i0, n1b, n_grid1, n_grid2, n_nuc, size_bh, r1, r2, rn, c_bh, m_bh,
-                         n_bh, o_bh, a_en, a_ee, grad1u);
+    return run_pair_only(E, E->stream, i0, n1b, n_grid1, 0, n_grid2, n_grid2,
+                         (int64_t)n1b * n_grid2, n_nuc, size_bh, r1, r2, rn, c_bh, m_bh, n_bh,
+                         o_bh, a_en, a_ee, grad1u);
 }
 
 extern "C" int cutc_split_gemm_dev(int n_slices, int M, int N, long long K, const double *A,

@@ -74,6 +74,7 @@ struct Request {
     int int2e_layout = CUTC_INT2E_PQST;
     const cutc_basis *basis = nullptr;  // evaluates aos1 / aos2 when those are NULL
     uint64_t mol_tag = 0;  // non-zero: molecule arrays identical to earlier builds with this tag
+    int x_only = 0;        // X alone (int_2e output NULL): wr1, aos1 and I are not used
     cudaStream_t stream = nullptr;
     int n1 = 0, n2 = 0, nA = 0, nN = 0, nB = 0;
     const double *r1 = nullptr, *wr1 = nullptr, *r2 = nullptr, *wr2 = nullptr, *rn = nullptr;
@@ -92,6 +93,12 @@ size_t build_footprint(const Request &R, size_t tile_budget);
 int build_terms(const Request &R, std::vector<double> &coef, std::vector<int> &exps,
                 std::vector<int> &off);
 int run_build(Engine *E, const Request &R, cutc_stats *stats);
+// FP64 pair terms on device arrays: r1 rows [i0, i0 + n1b) (of n1) against r2 points
+// [j0, j0 + n2b), written to G[c * plane + i * ldg + j]; synchronous on st.
+int run_pair_only(Engine *E, cudaStream_t st, int i0, int n1b, int n1, int j0, int n2b,
+                  int64_t ldg, int64_t plane, int nN, int nB, const double *r1, const double *r2,
+                  const double *rn, const double *c_bh, const int *m_bh, const int *n_bh,
+                  const int *o_bh, double a_en, double a_ee, double *G);
 void note_launches(int n);
 long launches_so_far();
 

@@ -111,7 +111,9 @@ void cutc_default_options(cutc_options *opt);
 /*
  * cutc_int with options.  With opt->device_pointers = 1 all array arguments
  * (inputs and outputs) are device pointers on the current device and no
- * host<->device copies are made.  stats may be NULL.
+ * host<->device copies are made.  stats may be NULL.  int_2e_ao may be NULL:
+ * then only X is built (opt->x_components of them), and wr1 and aos_data1 are
+ * not read and may be NULL too.
  */
 int cutc_int_ex(const cutc_options *opt,
                 int n_grid1, int n_grid2, int n_ao, int n_nuc, int size_bh,
@@ -307,6 +309,62 @@ int cutc_x_ao_to_mo(int n_grid1, int n_ao, int n_mo, int components,
 void trans_inplace(double *data, int size);
 void trans_pqst_psqt_inplace(int size, double *data);
 void trans_pqst_psqt_copy(int size, double *data_old, double *data_new);
+
+/* The launch geometry argument of the reference's device-level entry points:
+ * the layout of CUDA's dim3 (three unsigned ints), so a caller passing a dim3
+ * by value is served unchanged. */
+typedef struct cutc_dim3 {
+    unsigned int x, y, z;
+} cutc_dim3;
+
+/* ---- the reference's device-level stages of cutc_int, under its names ------
+ * Same signatures and device-pointer arguments as the reference; the work is
+ * ordered on the legacy default stream; failures are recorded for
+ * cutc_last_error().  All FP64, a_en = a_ee = 1 as in the reference.
+ *
+ * cutc_int_bh (src/jast_bh.cu:268-303): the pair terms of r1 points
+ * [ii0, ii0 + n_grid1_eff) against r2 points [jj0, jj0 + n_grid2_eff), written
+ * to grad1_u12[c * n_grid1_tot * n_grid2_tot + i * n_grid2_tot + j] with c = 0..2
+ * the gradient and c = 3 -1/2 |grad1 u|^2.  dimGrid / dimBlock are validated
+ * like cutc_int's launch integers and otherwise ignored.  Returns when done.
+ *
+ * int_long_range (src/long_range_integ.cu:52-67):
+ * out[j + n_grid2_tot (b + n_ao a)] = wr2[jj0 + j] chi_a chi_b at r2 point
+ * jj0 + j, for j < n_grid2_eff; aos_data2 is (n_grid2, n_ao[, 4]).
+ * int_short_range_herm (src/short_range_integ_herm.cu:51-64):
+ * out[g + n_grid1 (b + n_ao a)] = wr1 chi_a chi_b.
+ * int_short_range_nonherm (src/short_range_integ_nonherm.cu:69-82):
+ * out[g + n_grid1 m + 3 n_grid1 (b + n_ao a)] = wr1 (chi_b d_m chi_a - chi_a d_m chi_b).
+ * These three are asynchronous, like the reference's.
+ *
+ * get_int2_grad1_u12_ao (src/build_int2_grad1_u12_ao.cu:9-347): X with all four
+ * components, int2_grad1_u12_ao(n_ao, n_ao, n_grid1, 4) column-major on the
+ * device; the streamed X build of cutc_int_ex (plain FP64, or the split form
+ * with CUTC_PRECISION=split).  Returns when done.
+ * get_int_2e_ao (src/build_int_2e_ao.cu:11-145): int_2e_ao = A + A^T with
+ * A = X_3 S0 - 1/2 sum_m X_m S_m from the caller's int2_grad1_u12(n_ao, n_ao,
+ * n_grid1, 4), in FP64.  Returns when done. */
+void cutc_int_bh(cutc_dim3 dimGrid, cutc_dim3 dimBlock,
+                 int ii0, int n_grid1_eff, int n_grid1_tot,
+                 int jj0, int n_grid2_eff, int n_grid2_tot,
+                 int n_nuc, int size_bh,
+                 double *r1, double *r2, double *rn,
+                 double *c_bh, int *m_bh, int *n_bh, int *o_bh,
+                 double *grad1_u12);
+void int_long_range(int jj0, int n_grid2_eff, int n_grid2_tot,
+                    int n_grid2, int n_ao, double *wr2, double *aos_data2,
+                    double *int_fct_long_range);
+void int_short_range_herm(int n_grid1, int n_ao, double *wr1, double *aos_data1,
+                          double *int_fct_short_range_herm);
+void int_short_range_nonherm(int n_grid1, int n_ao, double *wr1, double *aos_data1,
+                             double *int_fct_short_range_nonherm);
+void get_int2_grad1_u12_ao(cutc_dim3 dimGrid, cutc_dim3 dimBlock,
+                           int n_grid1, int n_grid2, int n_ao, int n_nuc, int size_bh,
+                           double *r1, double *r2, double *wr2, double *rn, double *aos_data2,
+                           double *c_bh, int *m_bh, int *n_bh, int *o_bh,
+                           double *int2_grad1_u12_ao);
+void get_int_2e_ao(int n_grid1, int n_ao, double *wr1, double *aos_data1,
+                   double *int2_grad1_u12, double *int_2e_ao);
 
 /* Message describing the last non-zero status returned on this thread. */
 const char *cutc_last_error(void);
