@@ -301,14 +301,21 @@ pair_df_kernel(PairDfArgs P)
         for (int c = 0; c < 4; c++)
             P.G[o + c * P.plane] = w4[c];
         if (P.rmax) {
-            // row maxima for the slicer: the exponent of max |G| is that of the
-            // largest high word; one atomic per converged lane group and row
+            // row maxima for the slicer, which needs only an exponent e with
+            // |G| < 2^e: the high word of the double |hi| (hi + lo rounds to hi,
+            // so |hi + lo| never has a larger exponent), built from the float's
+            // bits with integer operations -- no FP64 on GB300's slow FP64 pipe.
+            // Float subnormals count as 2^-126.  One atomic per converged lane
+            // group and row.
             const unsigned mask = __activemask();
             const bool leader = (int)(threadIdx.x & 31) == __ffs(mask) - 1;
 #pragma unroll
             for (int c = 0; c < 4; c++) {
-                const double v = fabs((double)w4[c].x + (double)w4[c].y);
-                const unsigned hw = (unsigned)((unsigned long long)__double_as_longlong(v) >> 32);
+                const unsigned fb = __float_as_uint(w4[c].x) & 0x7fffffffu;
+                const unsigned ef = fb >> 23;
+                const unsigned hw = fb == 0u ? 0u
+                                  : ef == 0u ? (897u << 20)
+                                             : ((ef + 896u) << 20) | ((fb & 0x7fffffu) >> 3);
                 const unsigned m = __reduce_max_sync(mask, hw);
                 if (leader && m)
                     atomicMax(&P.rmax[(int64_t)c * P.n1b + row0 + r], (unsigned long long)m << 32);
