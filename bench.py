@@ -46,6 +46,23 @@ def log(msg):
 _T0 = time.perf_counter()
 
 
+def max_over_ranks(x, dist, device):
+    """The largest of every rank's x (the timing rule: the slowest rank sets the
+    time); x itself without a process group."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, steps, seconds):
+    """Builds per second of the whole job: every rank ran `steps` builds and the
+    slowest one took `seconds`."""
+    return world * steps / seconds
+
+
 def workload_desc(name, p):
     return ("%s: %d nuclei, n_ao=%d, n_grid1=%d, n_grid2=%d, %d Jastrow terms/atom"
             % (name, p.n_nuc, p.n_ao, p.n_grid1, p.n_grid2, p.size_bh))
@@ -318,13 +335,9 @@ def run_ours(args):
     ev1.record(stream)
     barrier()
     clocks = sampler.stop()
-    elapsed_ms = ev0.elapsed_time(ev1)
-    t = torch.tensor([elapsed_ms], dtype=torch.float64, device=dev)
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
     ms_per_step = elapsed_ms / args.steps
-    value = world * args.steps / (elapsed_ms / 1e3)
+    value = whole_job_rate(world, args.steps, elapsed_ms / 1e3)
 
     # ---- end to end through the C-ABI with host buffers -------------------------
     def pinned(a):
@@ -357,11 +370,8 @@ def run_ours(args):
         for k, v in st.as_dict().items():
             e2e_phases[k] = e2e_phases.get(k, 0) + v / e2e_steps
     barrier()
-    e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-    if dist is not None:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world * e2e_steps / float(te.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    e2e_value = whole_job_rate(world, e2e_steps, e2e_s)
     h2d = (p.r1.nbytes + p.wr1.nbytes + p.r2.nbytes + p.wr2.nbytes + p.rn.nbytes + p.aos1.nbytes
            + p.aos2.nbytes // 4 + p.c_bh.nbytes + 3 * p.m_bh.nbytes)
     d2h = Xh.nbytes + Ih.nbytes
