@@ -349,14 +349,17 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 
 // Operand sources: value of row r, column k of an FP64 matrix.
 struct SrcDense {  // X[r * ld + k]
+    static constexpr bool kDoubleFloat = false;
     const double *X;
     int64_t ld;
     __device__ double operator()(int64_t r, int64_t k) const { return X[r * ld + k]; }
 };
 
-struct SrcDenseDF {  // hi + lo of X[r * ld + k] (exact in FP64)
+struct SrcDenseDF {  // hi + lo of X[r * ld + k]; the slicer reads the pair itself
+    static constexpr bool kDoubleFloat = true;
     const float2 *X;
     int64_t ld;
+    __device__ float2 pair(int64_t r, int64_t k) const { return X[r * ld + k]; }
     __device__ double operator()(int64_t r, int64_t k) const
     {
         const float2 v = X[r * ld + k];
@@ -365,6 +368,7 @@ struct SrcDenseDF {  // hi + lo of X[r * ld + k] (exact in FP64)
 };
 
 struct SrcSym {  // w[k] chi_a(k) chi_b(k), (a, b) = pairs[r]
+    static constexpr bool kDoubleFloat = false;
     const double *w, *chi;
     int64_t ldchi;
     const int2 *pairs;
@@ -377,6 +381,7 @@ struct SrcSym {  // w[k] chi_a(k) chi_b(k), (a, b) = pairs[r]
 };
 
 struct SrcAnti {  // w (chi_c d_m chi_d - chi_d d_m chi_c), k = m n + g, (c, d) = pairs[r]
+    static constexpr bool kDoubleFloat = false;
     const double *w, *aos;  // aos: (ld, nA, 4) with the grid offset already applied
     int n, nA;              // n: grid points counted in k (g < n)
     int64_t ld;             // grid stride of aos
@@ -448,11 +453,14 @@ __device__ __forceinline__ int row_exponent(unsigned long long bits)
     return E == 0 ? 0 : E - 1022;
 }
 
-// The S signed base-2^9 digits of x 2^{-e} (first digit scaled by 2^8),
-// computed in 64-bit integer arithmetic and returned as exact BF16 values
-// q_s 2^{-8-9s}.
+// The S signed base-2^9 digits of x 2^{-e} (first digit scaled by 2^8), computed
+// in 64-bit integer arithmetic and returned as exact BF16 values q_s 2^{-8-9s}.
 template <int S>
-__device__ __forceinline__ void split_digits(double x, int e, __nv_bfloat16 (&out)[S])
+__device__ __forceinline__ void digits_of(long long t, __nv_bfloat16 (&out)[S]);
+
+// t = sign(x) floor(|x| 2^(F - e) + 1/2), F = 8 + 9 (S - 1): x rounded at its last digit
+template <int S>
+__device__ __forceinline__ long long scaled_round(double x, int e)
 {
     constexpr int F = 8 + 9 * (S - 1);
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
@@ -470,6 +478,61 @@ __device__ __forceinline__ void split_digits(double x, int e, __nv_bfloat16 (&ou
             T = 0;
         t = (bits >> 63) ? -(long long)T : (long long)T;
     }
+    return t;
+}
+
+// The same rounding of the exact sum x = hi + lo of a normalised double-float
+// (|lo| <= ulp(hi) / 2), in integer arithmetic only: GB300 converts and adds
+// FP64 at 1/64 of its FP32 rate, which made the G slicer FP64-bound.  With
+// V = |x| 2^(F - e) = A 2^-Q + B 2^-Q, A = |hi| 2^(F - e + Q) an integer and B
+// the signed part of lo, floor(V 2^Q) = A + floor(B) and, as 2^(Q-1) is an
+// integer, floor(V + 1/2) = (floor(V 2^Q) + 2^(Q-1)) >> Q.
+template <int S>
+__device__ __forceinline__ long long scaled_round_df(float hi, float lo, int e)
+{
+    constexpr int F = 8 + 9 * (S - 1);
+    const unsigned hb = __float_as_uint(hi), lb = __float_as_uint(lo);
+    if ((hb & 0x7fffffffu) == 0u)
+        return 0;  // lo is zero too
+    const unsigned hexp = (hb >> 23) & 0xffu;
+    const unsigned long long mh = hexp ? ((hb & 0x7fffffu) | 0x800000u) : (hb & 0x7fffffu);
+    const int a = (hexp ? (int)hexp : 1) - 150 + F - e;  // |hi| 2^(F-e) = mh 2^a, a <= F - 23
+    const int Q = a < -1 ? -a : 1;
+    if (Q >= 26)
+        return 0;  // V < 2^(24 - Q) (1 + 2^-24) < 1/2
+    const unsigned long long A = mh << (a + Q);
+    long long fb = 0;
+    if ((lb & 0x7fffffffu) != 0u) {
+        const unsigned lexp = (lb >> 23) & 0xffu;
+        const unsigned long long ml = lexp ? ((lb & 0x7fffffu) | 0x800000u) : (lb & 0x7fffffu);
+        const int sh = (lexp ? (int)lexp : 1) - 150 + F - e + Q;  // |lo| 2^(F-e+Q) = ml 2^sh
+        const bool same = ((hb ^ lb) >> 31) == 0u;
+        if (sh >= 0) {  // not reached for a normalised pair (sh < 0)
+            const long long v = (long long)(ml << min(sh, 39));
+            fb = same ? v : -v;
+        } else {
+            const int k = -sh;
+            if (same)
+                fb = k >= 64 ? 0 : (long long)(ml >> k);
+            else
+                fb = k >= 64 ? -1 : -(long long)((ml + (1ull << k) - 1) >> k);
+        }
+    }
+    const unsigned long long T = A + (unsigned long long)fb;  // the true sum is in [0, 2^64)
+    const long long r = (long long)((T + (1ull << (Q - 1))) >> Q);
+    return (hb >> 31) ? -r : r;
+}
+
+template <int S>
+__device__ __forceinline__ void split_digits(double x, int e, __nv_bfloat16 (&out)[S])
+{
+    digits_of<S>(scaled_round<S>(x, e), out);
+}
+
+// The S signed digits of t (q_s in [-256, 255] for s > 0) as exact BF16 values q_s 2^{-8-9s}.
+template <int S>
+__device__ __forceinline__ void digits_of(long long t, __nv_bfloat16 (&out)[S])
+{
     int q[S];
 #pragma unroll
     for (int s = S - 1; s >= 1; s--) {
@@ -500,8 +563,13 @@ __global__ void slice_kernel(Src src, int M, int64_t K, int64_t Kpad, int Mpad,
     __nv_bfloat16 d[4][S];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        const double x = (r < M && k + q < K) ? src(r, k + q) : 0.0;
-        split_digits<S>(x, e, d[q]);
+        if constexpr (Src::kDoubleFloat) {
+            const float2 v = (r < M && k + q < K) ? src.pair(r, k + q) : make_float2(0.f, 0.f);
+            digits_of<S>(scaled_round_df<S>(v.x, v.y, e), d[q]);
+        } else {
+            const double x = (r < M && k + q < K) ? src(r, k + q) : 0.0;
+            split_digits<S>(x, e, d[q]);
+        }
     }
 #pragma unroll
     for (int s = 0; s < S; s++) {
