@@ -89,15 +89,17 @@ static size_t mol_bytes(int n1, int n2, int nA, int nN)
             (size_t)n2 * nA) * sizeof(double);
 }
 
-// Frees unreferenced molecules, least recently used first, until `need` more
-// bytes fit in the cache budget.  Called with the lock held.
-static void evict_for(Server *S, size_t need)
+// Drops unreferenced molecules, least recently used first, until `need` more
+// bytes fit in the cache budget; their device buffers go to `to_free`, which the
+// caller frees after releasing the lock (cudaFree waits for the device, and the
+// other workers must not wait for it too).  Called with the lock held.
+static void evict_for(Server *S, size_t need, std::vector<void *> &to_free)
 {
     for (auto it = S->lru.end(); it != S->lru.begin() && S->cache_bytes + need > S->cfg.cache_budget_bytes;) {
         --it;
         MolEntry *m = *it;
         if (m->refs == 0) {
-            cudaFree(m->buf);
+            to_free.push_back(m->buf);
             S->cache_bytes -= m->bytes;
             S->mols.erase(m->key);
             it = S->lru.erase(it);
@@ -112,6 +114,7 @@ static int acquire_molecule(Server *S, Engine *E, const cutc_request &q, MolEntr
 {
     MolEntry *m = nullptr;
     bool upload = false;
+    std::vector<void *> to_free;  // evicted buffers, freed once the lock is released
     {
         std::unique_lock<std::mutex> lk(S->mu);
         auto it = S->mols.find(q.molecule_key);
@@ -132,7 +135,7 @@ static int acquire_molecule(Server *S, Engine *E, const cutc_request &q, MolEntr
             }
         } else {
             const size_t bytes = mol_bytes(q.n_grid1, q.n_grid2, q.n_ao, q.n_nuc);
-            evict_for(S, bytes);
+            evict_for(S, bytes, to_free);
             m = new MolEntry();
             m->key = q.molecule_key;
             m->n1 = q.n_grid1; m->n2 = q.n_grid2; m->nA = q.n_ao; m->nN = q.n_nuc;
@@ -144,7 +147,7 @@ static int acquire_molecule(Server *S, Engine *E, const cutc_request &q, MolEntr
                 if (old->refs == 0) {
                     S->lru.remove(old);
                     S->cache_bytes -= old->bytes;
-                    cudaFree(old->buf);
+                    to_free.push_back(old->buf);
                     delete old;
                 }
             }
@@ -156,6 +159,8 @@ static int acquire_molecule(Server *S, Engine *E, const cutc_request &q, MolEntr
             upload = true;
         }
     }
+    for (void *p : to_free)
+        cudaFree(p);
     if (upload) {
         auto finish = [&](int status) {
             std::lock_guard<std::mutex> lk(S->mu);
@@ -219,17 +224,22 @@ static int acquire_molecule(Server *S, Engine *E, const cutc_request &q, MolEntr
 
 static void release_molecule(Server *S, MolEntry *m)
 {
-    std::lock_guard<std::mutex> lk(S->mu);
-    m->refs--;
-    auto it = S->mols.find(m->key);
-    if (it == S->mols.end() || it->second != m) {
-        if (m->refs == 0) {  // replaced while in use
-            S->lru.remove(m);
-            S->cache_bytes -= m->bytes;
-            cudaFree(m->buf);
-            delete m;
+    void *to_free = nullptr;  // freed after the lock is released
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        m->refs--;
+        auto it = S->mols.find(m->key);
+        if (it == S->mols.end() || it->second != m) {
+            if (m->refs == 0) {  // replaced while in use
+                S->lru.remove(m);
+                S->cache_bytes -= m->bytes;
+                to_free = m->buf;
+                delete m;
+            }
         }
     }
+    if (to_free)
+        cudaFree(to_free);
 }
 
 static Request to_request(const cutc_request &q)
