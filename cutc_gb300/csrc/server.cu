@@ -26,6 +26,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -56,6 +57,7 @@ struct Job {
     int status = 1;  // 1 = pending
     Clock::time_point t_submit, t_start, t_end;
     bool cache_hit = false;
+    std::string message;  // the worker's error message when status is non-zero
 };
 
 struct Server {
@@ -310,8 +312,11 @@ static void worker(Server *S, int slot)
         }
         if (status == CUTC_OK)
             status = run_build(E, R, nullptr);
-        if (status != CUTC_OK)
+        std::string message;
+        if (status != CUTC_OK) {
+            message = cutc_last_error();  // this worker thread's message, for the waiter
             cudaStreamSynchronize(E->stream);
+        }
         if (m)
             release_molecule(S, m);
         bool release = false;
@@ -319,6 +324,7 @@ static void worker(Server *S, int slot)
         {
             std::lock_guard<std::mutex> lk(S->mu);
             job->t_end = Clock::now();
+            job->message = message;
             job->status = status;  // job may be freed by its waiter from here on
             if (status == CUTC_OK) {
                 S->completed++;
@@ -457,6 +463,8 @@ extern "C" int cutc_server_wait(cutc_server *h, unsigned long long ticket, doubl
     const int st = job->status;
     if (latency_ms)
         *latency_ms = std::chrono::duration<double, std::milli>(job->t_end - job->t_submit).count();
+    if (st != CUTC_OK)  // the cause, recorded by the worker, becomes this thread's message
+        cutc_set_error(st, "request %llu: %s", ticket, job->message.c_str());
     S->jobs.erase(it);
     return st;
 }

@@ -76,6 +76,7 @@ def test_failed_request_is_isolated():
         with pytest.raises(cg.CutcError) as e:
             srv.wait(tb)
         assert e.value.status == cg.CUTC_ERR_INVALID
+        assert "exponent" in str(e.value)  # the worker's message reaches the waiting thread
         for (p, key, prec), t in zip(reqs, tickets):
             X, I, _ = srv.wait(t)
             Xs, Is = cg.build_integrals(p, prec)
