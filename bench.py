@@ -35,8 +35,9 @@ from cutc_gb300 import synth  # noqa: E402
 
 METRIC = "TC integral builds/s (split-precision vs FP64 at 1e-10 rel err)"
 UNIT = "builds/s"
-CPU_SAMPLE_ROWS = 48        # per step of --impl reference
-CPU_BASELINE_ROWS = 256     # the cpu_baseline leg: about 10 s of oracle work on 16 cores
+CPU_SAMPLE_ROWS = 256       # per step of --impl reference: about 6 s of oracle work on 16 cores
+CPU_BASELINE_ROWS = 384     # the cpu_baseline leg: about 10 s; smaller samples underrate the
+                            # CPU (48 rows gave 0.00096 builds/s, 256 rows 0.00168)
 
 
 def log(msg):
