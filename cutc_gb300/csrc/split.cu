@@ -60,6 +60,14 @@ constexpr int kBM = 128;        // rows of A per CTA (TMEM lanes)
 constexpr int kBK = 32;         // K per TMA box: 32 BF16 = 64-byte rows (64B swizzle)
 constexpr int kChunkBlocks = 4; // exact-accumulation chunk: 128 K
 constexpr int kMaxKPerLaunch = 1 << 18;  // keeps every exact (hi, lo) sum below 2^24 units
+// Default K per launch: one launch up to kLongK; a longer contraction runs as equal
+// launches of at most kLaunchK, summed in FP64 (the C += epilogue).  On one GB300 the
+// X contraction of the 300-AO molecule (K = 200 000, 1500 r1 rows) took 1826 ms in one
+// launch and 1282 ms in five of 40 000; the medium one (K = 80 000) 1176 and 1168 ms
+// in one and two launches, and 1205 ms in three.  Over a long K loop the CTAs of a
+// wave probably drift apart and stop sharing their A and B tiles in L2.
+constexpr int kLongK = 65536;
+constexpr int kLaunchK = 49152;
 constexpr uint32_t kTmemCols = 512;
 constexpr int kGroupM = 8;      // row tiles per raster group (A tiles shared through L2)
 
@@ -751,8 +759,14 @@ static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alph
     CUTC_TRY(make_tmap(&ta, A.sl, (int64_t)S * A.Mpad, A.Kpad, kBM));
     CUTC_TRY(make_tmap(&tb, B.sl, (int64_t)S * B.Mpad, B.Kpad, Cfg::kBN));
     const int nkb_total = (int)(A.Kpad / kBK);
-    const int kmax = (k_split > 0 && k_split < kMaxKPerLaunch) ? k_split : kMaxKPerLaunch;
-    const int kb_per = std::max(1, kmax / kBK);
+    int kb_per;
+    if (k_split > 0) {
+        kb_per = std::max(1, std::min(k_split, kMaxKPerLaunch) / kBK);
+    } else {
+        const int64_t kt = (int64_t)nkb_total * kBK;
+        const int launches = kt <= kLongK ? 1 : (int)((kt + kLaunchK - 1) / kLaunchK);
+        kb_per = (nkb_total + launches - 1) / launches;
+    }
     if (A.Mpad % kBM || B.Mpad % Cfg::kBN) {
         cutc_set_error(CUTC_ERR_INVALID, "operand padding does not match the tile");
         return CUTC_ERR_INVALID;

@@ -81,7 +81,8 @@ typedef struct cutc_options {
     void *stream;           /* cudaStream_t to run on; NULL = the engine's stream */
     int pair_fp64;          /* split form: 1 = pair terms in FP64 instead of double-float */
     int k_split;            /* split form: max K per tensor-core launch; the partial results
-                               are summed in FP64 (0 = 262144) */
+                               are summed in FP64 (0 = automatic: one launch up to K = 65536,
+                               equal launches of at most 49152 beyond) */
     int int2e_layout;       /* CUTC_INT2E_PQST (reference order) or CUTC_INT2E_PSQT: int_2e with
                                its 2nd and 3rd indices swapped, as trans_pqst_psqt_inplace
                                leaves it (the order cutc_no uses), written directly */
