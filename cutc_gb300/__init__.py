@@ -51,7 +51,8 @@ class PlanInfo(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int) for k in ("tile_rows", "block_rows", "n_tiles", "n_blocks",
                                             "slab_cols")] + \
                [(k, ctypes.c_size_t) for k in ("budget_bytes", "fixed_bytes", "tile_row_bytes",
-                                               "block_row_bytes", "footprint_bytes")]
+                                               "block_row_bytes", "footprint_bytes")] + \
+               [("x_launches_per_tile", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -340,9 +341,11 @@ class PinnedArray:
 
 
 def plan(n_grid1, n_grid2, n_ao, n_nuc, precision=PLAIN_FP64, n_slices=None, x_components=3,
-         device_pointers=False, max_work_bytes=0) -> dict:
-    """The device-memory plan of a build (cutc_plan): tiles, blocks and bytes."""
-    opt = options(precision, n_slices, 1.0, 1.0, x_components, device_pointers, max_work_bytes)
+         device_pointers=False, max_work_bytes=0, k_split=0) -> dict:
+    """The device-memory plan of a build (cutc_plan): tiles, blocks, bytes and the
+    tensor-core launches per X contraction."""
+    opt = options(precision, n_slices, 1.0, 1.0, x_components, device_pointers, max_work_bytes,
+                  k_split=k_split)
     info = PlanInfo()
     s = load().cutc_plan(ctypes.byref(opt), n_grid1, n_grid2, n_ao, n_nuc, ctypes.byref(info))
     if s != CUTC_OK:

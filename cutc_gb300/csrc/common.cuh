@@ -5,6 +5,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
+
 #include "cutc_int.h"
 
 #define CUTC_CUDA_TRY(expr)                                                   \
@@ -61,5 +63,15 @@ inline unsigned ceil_div(int64_t a, int64_t b) { return (unsigned)((a + b - 1) /
 
 // Counts kernel launches of this library (reported in cutc_stats).
 void note_launches(int n);
+
+// The bit of the current device in a per-device "done" mask.  Function
+// attributes (the dynamic shared-memory opt-in) are set per device, so a flag
+// kept for the whole process would skip a second device.
+inline unsigned long long current_device_bit()
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return 1ull << (dev & 63);
+}
 
 }  // namespace cutc

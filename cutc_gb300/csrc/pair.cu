@@ -222,11 +222,12 @@ int launch_pair_f64(cudaStream_t st, const PairArgs &P)
     if (P.n1b <= 0 || P.n2 <= 0)
         return CUTC_OK;
     size_t smem = pair_f64_smem(P.n_terms, P.nN);
-    static bool attr_set = false;
-    if (!attr_set) {
+    static std::atomic<unsigned long long> attr_done{0};
+    const unsigned long long bit = current_device_bit();
+    if (!(attr_done.load() & bit)) {
         CUTC_CUDA_TRY(cudaFuncSetAttribute(pair_f64_kernel,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        attr_set = true;
+        attr_done.fetch_or(bit);
     }
     if (smem > 220 * 1024) {
         cutc_set_error(CUTC_ERR_INVALID, "too many nuclei/terms for the pair kernel (%zu B smem)", smem);

@@ -392,11 +392,12 @@ static int launch_df_impl(cudaStream_t st, PairDfArgs P, const double *rn, doubl
     }
     P.rows_per_cta = rows;
     const size_t smem = rows * per_row;
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<unsigned long long> attr_done{0};
+    const unsigned long long bit = current_device_bit();
+    if (!(attr_done.load() & bit)) {
         CUTC_CUDA_TRY(cudaFuncSetAttribute(pair_df_kernel<E, Sp>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        attr = true;
+        attr_done.fetch_or(bit);
     }
     dim3 grid(ceil_div(P.n2, kDfThreads), ceil_div(P.n1b, rows));
     pair_df_kernel<E, Sp><<<grid, kDfThreads, smem, st>>>(P);

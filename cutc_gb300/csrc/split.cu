@@ -742,6 +742,16 @@ static int slice_cols(cudaStream_t st, const double *X, int64_t ld, int64_t k0, 
     return CUTC_OK;
 }
 
+int split_k_blocks_per_launch(int64_t K, int k_split)
+{
+    const int64_t nkb_total = (std::max<int64_t>(K, 1) + kBK - 1) / kBK;
+    if (k_split > 0)
+        return std::max(1, std::min(k_split, kMaxKPerLaunch) / kBK);
+    const int64_t kt = nkb_total * kBK;
+    const int64_t launches = kt <= kLongK ? 1 : (kt + kLaunchK - 1) / kLaunchK;
+    return (int)((nkb_total + launches - 1) / launches);
+}
+
 // C = alpha A B^T (+ C) over the operands' common K.
 template <int S>
 static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alpha, double *C,
@@ -749,24 +759,18 @@ static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alph
                 int *err, int k_split = 0)
 {
     using Cfg = GemmCfg<S>;
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<unsigned long long> attr_done{0};
+    const unsigned long long bit = current_device_bit();
+    if (!(attr_done.load() & bit)) {
         CUTC_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<S>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem));
-        attr = true;
+        attr_done.fetch_or(bit);
     }
     CUtensorMap ta, tb;
     CUTC_TRY(make_tmap(&ta, A.sl, (int64_t)S * A.Mpad, A.Kpad, kBM));
     CUTC_TRY(make_tmap(&tb, B.sl, (int64_t)S * B.Mpad, B.Kpad, Cfg::kBN));
     const int nkb_total = (int)(A.Kpad / kBK);
-    int kb_per;
-    if (k_split > 0) {
-        kb_per = std::max(1, std::min(k_split, kMaxKPerLaunch) / kBK);
-    } else {
-        const int64_t kt = (int64_t)nkb_total * kBK;
-        const int launches = kt <= kLongK ? 1 : (int)((kt + kLaunchK - 1) / kLaunchK);
-        kb_per = (nkb_total + launches - 1) / launches;
-    }
+    const int kb_per = split_k_blocks_per_launch(A.Kpad, k_split);
     if (A.Mpad % kBM || B.Mpad % Cfg::kBN) {
         cutc_set_error(CUTC_ERR_INVALID, "operand padding does not match the tile");
         return CUTC_ERR_INVALID;

@@ -270,6 +270,8 @@ typedef struct cutc_plan_info {
     int slab_cols;              /* int_2e columns per output slab (host outputs) */
     size_t budget_bytes;        /* the budget each of tile and block was sized to */
     size_t fixed_bytes, tile_row_bytes, block_row_bytes, footprint_bytes;
+    int x_launches_per_tile;    /* split form: tensor-core launches that share one X
+                                   contraction's K (opt->k_split; 0 = automatic) */
 } cutc_plan_info;
 
 int cutc_plan(const cutc_options *opt, int n_grid1, int n_grid2, int n_ao, int n_nuc,

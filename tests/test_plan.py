@@ -74,3 +74,18 @@ def test_plan_without_budget_needs_a_device():
     with pytest.raises(cg.CutcError) as e:
         cg.plan(100, 100, 5, 1)
     assert e.value.status == cg.CUTC_ERR_NO_DEVICE
+
+
+def test_x_contraction_launches_per_tile():
+    """Split form: one tensor-core launch up to K = n_grid2 = 65536, equal launches of
+    at most 49152 beyond (FP64 sums between them); an explicit k_split caps them."""
+    budget = 8 << 30
+    for n2, launches in ((12000, 1), (50000, 1), (65536, 1), (65537, 2), (80000, 2),
+                         (120000, 3), (200000, 5)):
+        info = cg.plan(500, n2, 20, 3, cg.SPLIT_BF16, 5, max_work_bytes=budget)
+        assert info["x_launches_per_tile"] == launches, (n2, info)
+    assert cg.plan(500, 80000, 20, 3, cg.SPLIT_BF16, 5, max_work_bytes=budget,
+                   k_split=16384)["x_launches_per_tile"] == 5
+    assert cg.plan(500, 200000, 20, 3, cg.SPLIT_BF16, 5, max_work_bytes=budget,
+                   k_split=300000)["x_launches_per_tile"] == 1
+    assert cg.plan(500, 200000, 20, 3, cg.PLAIN_FP64, max_work_bytes=budget)["x_launches_per_tile"] == 1
