@@ -1,0 +1,126 @@
+// Rounding an operand to its S signed base-2^9 digits, in integer arithmetic.
+//
+// An operand value x of a row with exponent e (|x| < 2^e) is rounded at its
+// last digit, t = sign(x) floor(|x| 2^(F - e) + 1/2) with F = 8 + 9 (S - 1),
+// and t is cut into digits q_0 .. q_{S-1} (q_s in [-256, 255] for s > 0) with
+// t = sum_s q_s 2^(9 (S - 1 - s)).  Everything here is integer work, callable
+// from device code (the slicing kernels) and from host code, where a plain C++
+// build checks it against exact arithmetic.
+#pragma once
+
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#define CUTC_HD __host__ __device__ __forceinline__
+#else
+#define CUTC_HD inline
+#endif
+
+namespace cutc {
+namespace digits {
+
+CUTC_HD unsigned float_bits(float x)
+{
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(x);
+#else
+    unsigned u;
+    memcpy(&u, &x, sizeof u);
+    return u;
+#endif
+}
+
+CUTC_HD unsigned long long double_bits(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return (unsigned long long)__double_as_longlong(x);
+#else
+    unsigned long long u;
+    memcpy(&u, &x, sizeof u);
+    return u;
+#endif
+}
+
+// t for an FP64 value x
+template <int S>
+CUTC_HD long long scaled_round(double x, int e)
+{
+    constexpr int F = 8 + 9 * (S - 1);
+    const unsigned long long bits = double_bits(x);
+    const int E = (int)((bits >> 52) & 0x7ff);
+    long long t = 0;
+    if (E != 0) {
+        const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+        const int sh = E - 1075 - e + F;
+        unsigned long long T;
+        if (sh >= 0)
+            T = mant << sh;  // < 2^F because |x| < 2^e
+        else if (sh > -64)
+            T = (mant + (1ull << (-sh - 1))) >> (-sh);
+        else
+            T = 0;
+        t = (bits >> 63) ? -(long long)T : (long long)T;
+    }
+    return t;
+}
+
+// t for the exact sum x = hi + lo of a normalised double-float (|lo| <= ulp(hi)/2),
+// with no FP64 arithmetic: GB300 converts and adds FP64 at 1/64 of its FP32 rate,
+// which made the G slicer FP64-bound.  With V = |x| 2^(F - e) = A 2^-Q + B 2^-Q,
+// A = |hi| 2^(F - e + Q) an integer and B the signed part of lo,
+// floor(V 2^Q) = A + floor(B) and, as 2^(Q-1) is an integer,
+// floor(V + 1/2) = (floor(V 2^Q) + 2^(Q-1)) >> Q.
+template <int S>
+CUTC_HD long long scaled_round_df(float hi, float lo, int e)
+{
+    constexpr int F = 8 + 9 * (S - 1);
+    const unsigned hb = float_bits(hi), lb = float_bits(lo);
+    if ((hb & 0x7fffffffu) == 0u)
+        return 0;  // lo is zero too
+    const unsigned hexp = (hb >> 23) & 0xffu;
+    const unsigned long long mh = hexp ? ((hb & 0x7fffffu) | 0x800000u) : (hb & 0x7fffffu);
+    const int a = (hexp ? (int)hexp : 1) - 150 + F - e;  // |hi| 2^(F-e) = mh 2^a, a <= F - 23
+    const int Q = a < -1 ? -a : 1;
+    if (Q >= 26)
+        return 0;  // V < 2^(24 - Q) (1 + 2^-24) < 1/2
+    const unsigned long long A = mh << (a + Q);
+    long long fb = 0;
+    if ((lb & 0x7fffffffu) != 0u) {
+        const unsigned lexp = (lb >> 23) & 0xffu;
+        const unsigned long long ml = lexp ? ((lb & 0x7fffffu) | 0x800000u) : (lb & 0x7fffffu);
+        const int sh = (lexp ? (int)lexp : 1) - 150 + F - e + Q;  // |lo| 2^(F-e+Q) = ml 2^sh
+        const bool same = ((hb ^ lb) >> 31) == 0u;
+        if (sh >= 0) {  // not reached for a normalised pair (sh < 0)
+            const long long v = (long long)(ml << (sh < 39 ? sh : 39));
+            fb = same ? v : -v;
+        } else {
+            const int k = -sh;
+            if (same)
+                fb = k >= 64 ? 0 : (long long)(ml >> k);
+            else
+                fb = k >= 64 ? -1 : -(long long)((ml + (1ull << k) - 1) >> k);
+        }
+    }
+    const unsigned long long T = A + (unsigned long long)fb;  // the true sum is in [0, 2^64)
+    const long long r = (long long)((T + (1ull << (Q - 1))) >> Q);
+    return (hb >> 31) ? -r : r;
+}
+
+// q_0 .. q_{S-1} of t
+template <int S>
+CUTC_HD void digits_int(long long t, int (&q)[S])
+{
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int s = S - 1; s >= 1; s--) {
+        const long long d = ((t + 256) & 511) - 256;
+        q[s] = (int)d;
+        t = (t - d) >> 9;
+    }
+    q[0] = (int)t;
+}
+
+}  // namespace digits
+}  // namespace cutc

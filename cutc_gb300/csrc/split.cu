@@ -46,6 +46,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "digits.cuh"
 #include "products.cuh"
 #include "split.cuh"
 #include "tc.cuh"
@@ -461,97 +462,22 @@ __device__ __forceinline__ int row_exponent(unsigned long long bits)
     return E == 0 ? 0 : E - 1022;
 }
 
-// The S signed base-2^9 digits of x 2^{-e} (first digit scaled by 2^8), computed
-// in 64-bit integer arithmetic and returned as exact BF16 values q_s 2^{-8-9s}.
-template <int S>
-__device__ __forceinline__ void digits_of(long long t, __nv_bfloat16 (&out)[S]);
-
-// t = sign(x) floor(|x| 2^(F - e) + 1/2), F = 8 + 9 (S - 1): x rounded at its last digit
-template <int S>
-__device__ __forceinline__ long long scaled_round(double x, int e)
-{
-    constexpr int F = 8 + 9 * (S - 1);
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    const int E = (int)((bits >> 52) & 0x7ff);
-    long long t = 0;
-    if (E != 0) {
-        const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-        const int sh = E - 1075 - e + F;
-        unsigned long long T;
-        if (sh >= 0)
-            T = mant << sh;  // < 2^F because |x| < 2^e
-        else if (sh > -64)
-            T = (mant + (1ull << (-sh - 1))) >> (-sh);
-        else
-            T = 0;
-        t = (bits >> 63) ? -(long long)T : (long long)T;
-    }
-    return t;
-}
-
-// The same rounding of the exact sum x = hi + lo of a normalised double-float
-// (|lo| <= ulp(hi) / 2), in integer arithmetic only: GB300 converts and adds
-// FP64 at 1/64 of its FP32 rate, which made the G slicer FP64-bound.  With
-// V = |x| 2^(F - e) = A 2^-Q + B 2^-Q, A = |hi| 2^(F - e + Q) an integer and B
-// the signed part of lo, floor(V 2^Q) = A + floor(B) and, as 2^(Q-1) is an
-// integer, floor(V + 1/2) = (floor(V 2^Q) + 2^(Q-1)) >> Q.
-template <int S>
-__device__ __forceinline__ long long scaled_round_df(float hi, float lo, int e)
-{
-    constexpr int F = 8 + 9 * (S - 1);
-    const unsigned hb = __float_as_uint(hi), lb = __float_as_uint(lo);
-    if ((hb & 0x7fffffffu) == 0u)
-        return 0;  // lo is zero too
-    const unsigned hexp = (hb >> 23) & 0xffu;
-    const unsigned long long mh = hexp ? ((hb & 0x7fffffu) | 0x800000u) : (hb & 0x7fffffu);
-    const int a = (hexp ? (int)hexp : 1) - 150 + F - e;  // |hi| 2^(F-e) = mh 2^a, a <= F - 23
-    const int Q = a < -1 ? -a : 1;
-    if (Q >= 26)
-        return 0;  // V < 2^(24 - Q) (1 + 2^-24) < 1/2
-    const unsigned long long A = mh << (a + Q);
-    long long fb = 0;
-    if ((lb & 0x7fffffffu) != 0u) {
-        const unsigned lexp = (lb >> 23) & 0xffu;
-        const unsigned long long ml = lexp ? ((lb & 0x7fffffu) | 0x800000u) : (lb & 0x7fffffu);
-        const int sh = (lexp ? (int)lexp : 1) - 150 + F - e + Q;  // |lo| 2^(F-e+Q) = ml 2^sh
-        const bool same = ((hb ^ lb) >> 31) == 0u;
-        if (sh >= 0) {  // not reached for a normalised pair (sh < 0)
-            const long long v = (long long)(ml << min(sh, 39));
-            fb = same ? v : -v;
-        } else {
-            const int k = -sh;
-            if (same)
-                fb = k >= 64 ? 0 : (long long)(ml >> k);
-            else
-                fb = k >= 64 ? -1 : -(long long)((ml + (1ull << k) - 1) >> k);
-        }
-    }
-    const unsigned long long T = A + (unsigned long long)fb;  // the true sum is in [0, 2^64)
-    const long long r = (long long)((T + (1ull << (Q - 1))) >> Q);
-    return (hb >> 31) ? -r : r;
-}
-
-template <int S>
-__device__ __forceinline__ void split_digits(double x, int e, __nv_bfloat16 (&out)[S])
-{
-    digits_of<S>(scaled_round<S>(x, e), out);
-}
-
-// The S signed digits of t (q_s in [-256, 255] for s > 0) as exact BF16 values q_s 2^{-8-9s}.
+// The S signed base-2^9 digits of t (digits.cuh) as exact BF16 values q_s 2^{-8-9s}.
 template <int S>
 __device__ __forceinline__ void digits_of(long long t, __nv_bfloat16 (&out)[S])
 {
     int q[S];
-#pragma unroll
-    for (int s = S - 1; s >= 1; s--) {
-        const long long d = ((t + 256) & 511) - 256;
-        q[s] = (int)d;
-        t = (t - d) >> 9;
-    }
-    q[0] = (int)t;
+    digits::digits_int<S>(t, q);
 #pragma unroll
     for (int s = 0; s < S; s++)
         out[s] = __float2bfloat16_rn(__int2float_rn(q[s]) * exp2f((float)(-8 - 9 * s)));
+}
+
+// The digits of an FP64 value x 2^{-e} (first digit scaled by 2^8).
+template <int S>
+__device__ __forceinline__ void split_digits(double x, int e, __nv_bfloat16 (&out)[S])
+{
+    digits_of<S>(digits::scaled_round<S>(x, e), out);
 }
 
 // slices[(s * Mpad + r) * Kpad + k] for r < Mpad, k < Kpad (zeros outside M x K);
@@ -573,7 +499,7 @@ __global__ void slice_kernel(Src src, int M, int64_t K, int64_t Kpad, int Mpad,
     for (int q = 0; q < 4; q++) {
         if constexpr (Src::kDoubleFloat) {
             const float2 v = (r < M && k + q < K) ? src.pair(r, k + q) : make_float2(0.f, 0.f);
-            digits_of<S>(scaled_round_df<S>(v.x, v.y, e), d[q]);
+            digits_of<S>(digits::scaled_round_df<S>(v.x, v.y, e), d[q]);
         } else {
             const double x = (r < M && k + q < K) ? src(r, k + q) : 0.0;
             split_digits<S>(x, e, d[q]);
