@@ -49,3 +49,37 @@ def test_no_device_is_a_status_not_an_exit():
     s = cg.cutc_int(1, 1, 1, 32, 1, 1, 2, 2, 1, 1, 1, z, z, z, z, z, z, z, z, zi, zi, zi, z, z)
     assert s == cg.CUTC_ERR_NO_DEVICE
     assert "device" in cg.last_error()
+
+
+# The reference's device-level stages: parameter names in the reference's order
+# (src/jast_bh.cu:268-272, src/long_range_integ.cu:52-54,
+# src/short_range_integ_herm.cu:51-52, src/short_range_integ_nonherm.cu:69-70,
+# src/build_int2_grad1_u12_ao.cu:9-13, src/build_int_2e_ao.cu:11-12).
+REFERENCE_STAGES = {
+    "cutc_int_bh": ["dimGrid", "dimBlock", "ii0", "n_grid1_eff", "n_grid1_tot", "jj0",
+                    "n_grid2_eff", "n_grid2_tot", "n_nuc", "size_bh", "r1", "r2", "rn", "c_bh",
+                    "m_bh", "n_bh", "o_bh", "grad1_u12"],
+    "int_long_range": ["jj0", "n_grid2_eff", "n_grid2_tot", "n_grid2", "n_ao", "wr2",
+                       "aos_data2", "int_fct_long_range"],
+    "int_short_range_herm": ["n_grid1", "n_ao", "wr1", "aos_data1", "int_fct_short_range_herm"],
+    "int_short_range_nonherm": ["n_grid1", "n_ao", "wr1", "aos_data1",
+                                "int_fct_short_range_nonherm"],
+    "get_int2_grad1_u12_ao": ["dimGrid", "dimBlock", "n_grid1", "n_grid2", "n_ao", "n_nuc",
+                              "size_bh", "r1", "r2", "wr2", "rn", "aos_data2", "c_bh", "m_bh",
+                              "n_bh", "o_bh", "int2_grad1_u12_ao"],
+    "get_int_2e_ao": ["n_grid1", "n_ao", "wr1", "aos_data1", "int2_grad1_u12", "int_2e_ao"],
+}
+
+
+def test_reference_stage_signatures():
+    text = open(os.path.join(ROOT, "include", "cutc_int.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    for name, want in REFERENCE_STAGES.items():
+        m = re.search(r"void %s\((.*?)\);" % name, text, flags=re.S)
+        assert m, name
+        params = [p.strip().split()[-1].lstrip("*") for p in m.group(1).split(",")]
+        assert params == want, (name, params)
+        # dim3 arguments are passed by value as three unsigned ints
+        if "dimGrid" in want:
+            assert re.search(r"cutc_dim3 dimGrid, cutc_dim3 dimBlock", m.group(1)), name
+    assert re.search(r"typedef struct cutc_dim3 \{\s*unsigned int x, y, z;\s*\} cutc_dim3;", text)
