@@ -83,3 +83,22 @@ def test_reference_stage_signatures():
         if "dimGrid" in want:
             assert re.search(r"cutc_dim3 dimGrid, cutc_dim3 dimBlock", m.group(1)), name
     assert re.search(r"typedef struct cutc_dim3 \{\s*unsigned int x, y, z;\s*\} cutc_dim3;", text)
+
+
+def test_header_compiles_as_c_and_cpp(tmp_path):
+    """include/cutc_int.h is a plain C header (the reference's callers are C and
+    Fortran) that also compiles as C++, warning-free in both."""
+    import shutil
+    import subprocess
+    src_c = tmp_path / "use.c"
+    src_c.write_text('#include "cutc_int.h"\nint main(void) { cutc_options o; '
+                     'cutc_default_options(&o); cutc_dim3 g = {1, 1, 1}; (void)g; '
+                     'return o.precision; }\n')
+    src_cpp = tmp_path / "use.cpp"
+    src_cpp.write_text(src_c.read_text())
+    inc = os.path.join(ROOT, "include")
+    for compiler, src, std in (("gcc", src_c, "-std=c99"), ("g++", src_cpp, "-std=c++17")):
+        if shutil.which(compiler) is None:
+            pytest.skip(compiler + " not available")
+        subprocess.check_call([compiler, std, "-Wall", "-Wextra", "-Werror", "-pedantic",
+                               "-fsyntax-only", "-I", inc, str(src)])

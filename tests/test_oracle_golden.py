@@ -52,3 +52,21 @@ def test_small_workload_digest():
     assert np.max(np.abs(A.ravel()[d["I_idx"]] - d["I_val"])) < 1e-12 * im
     assert abs(np.linalg.norm(X3.ravel()) - d["X_norm"]) < 1e-12 * d["X_norm"]
     assert abs(np.linalg.norm(A.ravel()) - d["I_norm"]) < 1e-12 * d["I_norm"]
+
+
+def test_oracle_pair_term_symmetries():
+    """Properties of the Boys-Handy form the oracle restates (src/jast_bh.cu:203-242):
+    swapping m and n in every term leaves u, hence G, unchanged, and scaling every
+    coefficient by k scales grad u by k and -1/2 |grad u|^2 by k^2."""
+    import dataclasses
+    from cutc_gb300 import synth
+    p = synth.make_problem(n_nuc=2, n_ao=3, n_grid1=40, n_grid2=60, size_bh=5, seed=31)
+    G = oracle.pair(p)
+    swapped = dataclasses.replace(p, m_bh=p.n_bh.copy(), n_bh=p.m_bh.copy())
+    assert np.array_equal(oracle.pair(swapped), G) or \
+        np.abs(oracle.pair(swapped) - G).max() <= 1e-15 * np.abs(G).max()
+    k = 0.75
+    scaled = dataclasses.replace(p, c_bh=p.c_bh * k)
+    Gs = oracle.pair(scaled)
+    np.testing.assert_allclose(Gs[:3], k * G[:3], rtol=0, atol=1e-14 * np.abs(G[:3]).max())
+    np.testing.assert_allclose(Gs[3], k * k * G[3], rtol=0, atol=1e-14 * np.abs(G[3]).max())
