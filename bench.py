@@ -12,13 +12,25 @@ C-ABI with host buffers, host<->device copies inside the timed region.
 ships no CPU path, so its arithmetic is transcribed and timed on a bounded
 sample of r1 rows, scaled to a full build.
 
+On one GPU the line also carries the rest of the metric, each measured in the
+same run: the error of both forms against the FP64 oracle (``accuracy``), the
+plain FP64 form's rate, the large workload on r1 samples (``large``), the
+Jastrow-parameter scan (``scan``), a prefix of the serving stream with p50/p99
+latency (``serving``) and the split contraction beside cuBLAS's own FP64
+emulation on the same operands (``rival``).
+
 Under torchrun (N > 1) every rank runs an independent replica of the workload
 (the path is single-GPU; there is no collective on the data path) and the
 reported value is the sum over ranks: weak scaling.
+
+Micro-benchmarks of single kernels (the cases the committed ncu summaries were
+captured on): ``--kernel split_gemm|fp64_gemm|pair|plain_build|rival``.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
+import dataclasses
 import json
 import os
 import subprocess
@@ -80,10 +92,31 @@ def measured_peaks():
 
 def sub_problem(p, i0, n):
     """The same molecule with r1 restricted to rows [i0, i0+n)."""
-    import dataclasses
     return dataclasses.replace(
         p, r1=np.ascontiguousarray(p.r1[i0:i0 + n]), wr1=np.ascontiguousarray(p.wr1[i0:i0 + n]),
         aos1=np.ascontiguousarray(p.aos1[:, :, i0:i0 + n]))
+
+
+def release_device():
+    import torch
+    import cutc_gb300 as cg
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    cg.load().cutc_release()
+
+
+def cuda_ms(fn, stream=None):
+    """Device time of fn() on `stream` (torch's current stream by default)."""
+    import torch
+    s = stream or torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    fn()
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
 
 def plain_rate_estimate(cg, p, sizes):
     """Plain FP64 builds/s of the full grid from device-timed builds on two r1
@@ -94,45 +127,38 @@ def plain_rate_estimate(cg, p, sizes):
     stream = torch.cuda.Stream(device=dev)
     opt = cg.options(cg.PLAIN_FP64, None, p.a_en, p.a_ee, 3, True, 0, stream.cuda_stream)
     Id = torch.empty((nA2, nA2), dtype=torch.float64, device=dev)
-    times = []
+    times, gemm = [], []
     for k, ns in enumerate(sizes):
-        sub = strided_rows(p, ns)
+        sub = synth.r1_sample(p, ns)
         dr = {key: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for key, v in sub.arrays().items()}
         Xd = torch.empty((3, ns, nA2), dtype=torch.float64, device=dev)
         reps = 2 if k == 0 else 1  # the first build also sets up the workspace
         for r in range(reps):
+            st = cg.Stats()
             torch.cuda.synchronize(dev)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             s = cg.cutc_int_ex(opt, ns, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
                                dr["r1"], dr["wr1"], dr["r2"], dr["wr2"], dr["rn"], dr["aos1"],
-                               dr["aos2"], dr["c_bh"], dr["m_bh"], dr["n_bh"], dr["o_bh"], Xd, Id, None)
+                               dr["aos2"], dr["c_bh"], dr["m_bh"], dr["n_bh"], dr["o_bh"], Xd, Id, st)
             e1.record(stream)
             torch.cuda.synchronize(dev)
             if s != cg.CUTC_OK:
                 raise cg.CutcError(s, cg.last_error())
         times.append(e0.elapsed_time(e1))
+        np_ = p.n_ao * (p.n_ao + 1) // 2
+        gemm.append(2.0 * np_ * 4 * ns * p.n_grid2 / (st.ms_x_gemm * 1e-3) / 1e12)
         del dr, Xd
     (n_a, n_b), (t_a, t_b) = sizes, times
     slope = (t_b - t_a) / (n_b - n_a)
     t_full = t_b + slope * (p.n_grid1 - n_b)
     del Id
-    torch.cuda.empty_cache()
-    cg.load().cutc_release()
+    release_device()
     return {"value_est": 1e3 / t_full, "unit": UNIT, "ms_per_build_est": t_full,
+            "x_gemm_fp64_tflops": gemm[-1],
+            "x_gemm_kernel": "fp64_gemm_kernel (DMMA m8n8k4 tiles, this library)",
             "basis": "plain FP64 form, device-resident, timed on %d and %d r1 rows (%.0f and %.0f ms) "
                      "and extrapolated linearly to n_grid1=%d" % (n_a, n_b, t_a, t_b, p.n_grid1)}
-
-
-def strided_rows(p, ns):
-    """The same molecule with ns r1 points spread evenly over the whole r1 grid
-    (every nucleus' shells are represented)."""
-    import dataclasses
-    idx = np.unique(np.linspace(0, p.n_grid1 - 1, ns).round().astype(np.int64))
-    assert len(idx) == ns
-    return dataclasses.replace(
-        p, r1=np.ascontiguousarray(p.r1[idx]), wr1=np.ascontiguousarray(p.wr1[idx]),
-        aos1=np.ascontiguousarray(p.aos1[:, :, idx]))
 
 
 # ---------------------------------------------------------------------------
@@ -193,36 +219,44 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def gpu_uuid(dev):
+    import torch
+    try:
+        return "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        return None
+
+
 # ---------------------------------------------------------------------------
 # CPU oracle leg (bounded sample)
 # ---------------------------------------------------------------------------
-def cpu_sample(p, rows=CPU_SAMPLE_ROWS, reps=1, offsets=(0,)):
-    """Time the oracle on `rows` r1 rows (pair terms, X, their int_2e share)
-    plus the r2-side products once; scale to the full build."""
+def cpu_sample(p, rows=CPU_SAMPLE_ROWS):
+    """Time the oracle on `rows` r1 rows spread over the grid (pair terms, X,
+    their int_2e share) plus the r2-side products once; scale to the full build.
+    Returns the cpu_baseline record and the oracle's outputs on the sample
+    (sub-problem, X (4, rows, nA^2), int_2e (nA^2, nA^2))."""
     from oracle import oracle
     t0 = time.perf_counter()
     P = oracle.long_range(p)
     t_p = time.perf_counter() - t0
-    times = []
-    for rep in range(reps):
-        i0 = offsets[rep % len(offsets)]
-        sub = sub_problem(p, i0, rows)
-        t0 = time.perf_counter()
-        X = oracle.x_block(sub, P, 0, rows)
-        oracle.int2e_from_x(sub, X)
-        times.append(time.perf_counter() - t0)
-    t_rows = float(np.mean(times))
+    sub = synth.r1_sample(p, rows)
+    t0 = time.perf_counter()
+    X4 = oracle.x_block(sub, P, 0, rows)
+    A = oracle.int2e_from_x(sub, X4)
+    t_rows = time.perf_counter() - t0
+    del P
     t_build = t_p + t_rows * p.n_grid1 / rows
-    return {
+    cb = {
         "value": 1.0 / t_build,
         "unit": UNIT,
         "cores": os.cpu_count(),
         "kind": "port",
-        "sample": ("%d of %d r1 rows (pair terms, X rows and their int_2e share, "
-                   "%d rep(s)) + the r2 pair products once; scaled by n_grid1/%d"
-                   % (rows, p.n_grid1, reps, rows)),
-        "seconds_timed": t_p + sum(times),
-    }, t_rows, t_p
+        "sample": ("%d of %d r1 rows spread over the grid (pair terms, X rows and their int_2e "
+                   "share) + the r2 pair products once; scaled by n_grid1/%d"
+                   % (rows, p.n_grid1, rows)),
+        "seconds_timed": t_p + t_rows,
+    }
+    return cb, sub, X4, A + A.T
 
 
 def run_reference(args):
@@ -236,7 +270,7 @@ def run_reference(args):
     t0 = time.perf_counter()
     P = oracle.long_range(p)
     t_p = time.perf_counter() - t0
-    rows = CPU_SAMPLE_ROWS
+    rows = min(CPU_SAMPLE_ROWS, p.n_grid1)
     step_times = []
     for step in range(args.warmup + args.steps):
         i0 = (step * 997 * rows) % max(1, p.n_grid1 - rows)
@@ -313,12 +347,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         build_device()
     log("timed region")
-    uuid = None
-    try:
-        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
-    except Exception:
-        uuid = None
-    sampler = ClockSampler(uuid)
+    sampler = ClockSampler(gpu_uuid(dev))
     sampler.start()
     time.sleep(0.5)
     barrier()
@@ -376,6 +405,7 @@ def run_ours(args):
     h2d = (p.r1.nbytes + p.wr1.nbytes + p.r2.nbytes + p.wr2.nbytes + p.rn.nbytes + p.aos1.nbytes
            + p.aos2.nbytes // 4 + p.c_bh.nbytes + 3 * p.m_bh.nbytes)
     d2h = Xh.nbytes + Ih.nbytes
+    del hp, Xh, Ih
 
     # ---- the unmodified drop-in call: cutc_int, pageable arrays, form from the env --------
     drop_in = None
@@ -410,7 +440,9 @@ def run_ours(args):
             del os.environ["CUTC_PRECISION"]
         else:
             os.environ["CUTC_PRECISION"] = prev
+        del Xp, Ip, ha
         log("drop-in cutc_int, pageable arrays: %.3f builds/s" % drop_in["value"])
+    log("e2e: %.3f builds/s" % e2e_value)
 
     out = None
     if rank == 0:
@@ -453,24 +485,44 @@ def run_ours(args):
                "e2e_drop_in": drop_in,
                "phases_ms_per_step": {"pair": pair_ms / args.steps,
                                       "x_gemm": gemm_ms / args.steps}}
-    # ---- accuracy and the plain FP64 rate on an r1 sample --------------------------
-    log("e2e: %.3f builds/s" % e2e_value)
-    if rank == 0 and not args.skip_accuracy:
-        log("accuracy / plain sample")
-        rows = 256
-        sub = sub_problem(p, (p.n_grid1 // 2) // 64 * 64, rows)
-        Xs, Is = cg.build_integrals(sub, cg.SPLIT_BF16, n_slices=args.slices)
-        Xp, Ip = cg.build_integrals(sub, cg.PLAIN_FP64)
-        from oracle.oracle import rel_err
-        out["accuracy"] = {"X_vs_fp64": rel_err(Xs, Xp), "int2e_vs_fp64": rel_err(Is, Ip),
-                           "sample": "%d of %d r1 rows of the workload; split (%d slices) vs "
-                                     "the plain FP64 form (itself 1e-12 from the oracle)"
-                                     % (rows, p.n_grid1, args.slices)}
-        out["plain_fp64"] = plain_rate_estimate(cg, p, (rows, 2 * rows))
-    if rank == 0 and world == 1 and not args.skip_cpu:
+    one_gpu = rank == 0 and world == 1
+    if one_gpu and not args.skip_rival:
+        log("rival: cuBLAS FP64 emulation vs the split contraction")
+        out["rival"] = guarded(rival_leg, cg, p, dr, Xd, args.slices)
+    del dr, Xd, Id
+    release_device()
+
+    # ---- the CPU oracle: baseline timing and the accuracy of both forms -------------
+    if one_gpu and not args.skip_cpu:
         log("cpu baseline sample")
-        cb, _, _ = cpu_sample(p, rows=min(CPU_BASELINE_ROWS, p.n_grid1))
+        cb, sub, Xo, Io = cpu_sample(p, rows=min(CPU_BASELINE_ROWS, p.n_grid1))
         out["cpu_baseline"] = cb
+        if not args.skip_accuracy:
+            log("accuracy of both forms vs the oracle")
+            acc = {"sample": "%d of %d r1 rows spread over the grid; both forms against the FP64 "
+                             "oracle (oracle/, C restatement of the reference's kernels + numpy "
+                             "DGEMM)" % (sub.n_grid1, p.n_grid1)}
+            for name, pr in (("split", cg.SPLIT_BF16), ("plain", cg.PLAIN_FP64)):
+                X, I = cg.build_integrals(sub, pr, n_slices=args.slices if pr else None)
+                acc[name] = {"X_vs_oracle": rel(X, Xo[:3]), "int2e_vs_oracle": rel(I, Io)}
+                del X, I
+            out["accuracy"] = acc
+        del Xo, Io
+        release_device()
+    if one_gpu and not args.skip_accuracy:
+        log("plain FP64 rate")
+        out["plain_fp64"] = guarded(plain_rate_estimate, cg, p, (256, 512))
+    if one_gpu and not args.skip_large:
+        log("large workload on r1 samples")
+        out["large"] = guarded(large_leg, cg, args, 1, 1, not args.skip_accuracy)
+    if one_gpu and not args.skip_scan:
+        log("Jastrow-parameter scan")
+        out["scan"] = guarded(scan_leg, cg, args, 16, not args.skip_accuracy)
+    if one_gpu and not args.skip_serving:
+        log("serving stream prefix")
+        plain_tf = (out.get("plain_fp64") or {}).get("x_gemm_fp64_tflops")
+        out["serving"] = guarded(serving_leg, cg, args, 32, 1.0, 250, not args.skip_accuracy,
+                                 plain_tf)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist is not None:
@@ -479,10 +531,29 @@ def run_ours(args):
     return 0
 
 
+def rel(a, b):
+    from oracle.oracle import rel_err
+    return rel_err(a, b)
+
+
+def guarded(fn, *a):
+    """One extra leg of the line: its record, or the error that stopped it (the
+    main measurement stands either way)."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001
+        log("leg %s failed: %r" % (fn.__name__, e))
+        try:
+            release_device()
+        except Exception:  # noqa: BLE001
+            pass
+        return {"error": repr(e)[:400]}
+
+
 # ---------------------------------------------------------------------------
 # the large workload: r1 samples of the full molecule and grids
 # ---------------------------------------------------------------------------
-def run_large(args):
+def large_leg(cg, args, warmup, steps, with_accuracy, sizes=(3000, 6000)):
     """Large workload (n_ao=300, n_grid2=200,000) timed on two r1 samples spread
     over the 60,000-point r1 grid and extrapolated linearly in n_grid1.
 
@@ -493,28 +564,20 @@ def run_large(args):
     assembly), which the two samples separate.
     """
     import torch
-    import cutc_gb300 as cg
-
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
+    dev = torch.device("cuda", torch.cuda.current_device())
     prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
-    p = synth.make_config(args.config)
+    p = synth.make_config("large")
     nA2 = p.n_ao ** 2
-    sizes = (args.r1_sample // 2, args.r1_sample)
     stream = torch.cuda.Stream(device=dev)
     opt = cg.options(prec, args.slices, p.a_en, p.a_ee, 3, True, 0, stream.cuda_stream,
                      k_split=args.k_split)
+    release_device()
     Id = torch.empty((nA2, nA2), dtype=torch.float64, device=dev)
-    uuid = None
-    try:
-        uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
-    except Exception:
-        pass
     samples = []
     gemm_ms, gemm_launches, launches, pair_ms, flops_x = 0.0, 0, 0, 0.0, 0.0
-    sampler = ClockSampler(uuid)
+    sampler = ClockSampler(gpu_uuid(dev))
     for ns in sizes:
-        sub = strided_rows(p, ns)
+        sub = synth.r1_sample(p, ns)
         dr = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in sub.arrays().items()}
         Xd = torch.empty((3, ns, nA2), dtype=torch.float64, device=dev)
 
@@ -527,7 +590,7 @@ def run_large(args):
                 raise cg.CutcError(s, cg.last_error())
 
         log("large: %d r1 rows, warm-up" % ns)
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             build()
         if ns == sizes[-1]:
             sampler.start()
@@ -536,7 +599,7 @@ def run_large(args):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         tiles = 0
-        for _ in range(args.steps):
+        for _ in range(steps):
             st = cg.Stats()
             build(st)
             tiles = st.n_r1_tiles
@@ -548,14 +611,13 @@ def run_large(args):
                 flops_x += 8.0 * nA2 * ns * p.n_grid2
         e1.record(stream)
         torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1) / args.steps
+        ms = e0.elapsed_time(e1) / steps
         samples.append({"r1_rows": ns, "ms_per_build": ms, "r1_tiles": tiles})
         log("large: %d rows: %.1f ms per build" % (ns, ms))
         del dr, Xd
     clocks = sampler.stop()
     del Id
-    torch.cuda.empty_cache()
-    cg.load().cutc_release()
+    release_device()
     (n_a, n_b), (t_a, t_b) = sizes, (samples[0]["ms_per_build"], samples[1]["ms_per_build"])
     slope = (t_b - t_a) / (n_b - n_a)
     t_full = t_b + slope * (p.n_grid1 - n_b)
@@ -569,95 +631,133 @@ def run_large(args):
     n_products = S * (S + 1) // 2 if prec == cg.SPLIT_BF16 else 0
     packed = p.n_ao * (p.n_ao + 1) / 2.0 / nA2
     executed = achieved * packed * n_products if n_products else None
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": t_full, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None,
-           "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
-           "config": {"workload": workload_desc(args.config, p), "precision": args.precision,
-                      "n_slices": S if prec else None,
-                      "projection": "device-resident builds on %d and %d r1 rows spread over the "
-                                    "r1 grid, extrapolated linearly to n_grid1=%d"
-                                    % (n_a, n_b, p.n_grid1),
-                      "l2": "inputs larger than L2: P slices alone are %.0f GB" %
-                            (2 * S * p.n_ao * (p.n_ao + 1) / 2 * p.n_grid2 / 1e9),
-                      "parallelism": "1 GPU"},
+    out = {"value": value, "unit": UNIT, "ms_per_build": t_full,
+           "workload": workload_desc("large", p), "precision": args.precision,
+           "projection": "device-resident builds on %d and %d r1 rows spread over the r1 grid "
+                         "(%d warm-up, %d timed each), extrapolated linearly to n_grid1=%d"
+                         % (n_a, n_b, warmup, steps, p.n_grid1),
            "samples": samples, "gpu_launches": launches, "clocks": clocks,
-           "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                        "frac": achieved / peak, "traffic": None,
-                        "kernel": "split_gemm_kernel (X build, one launch per r1 tile)",
+           "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                        "unit": "TFLOP/s", "frac": achieved / peak,
+                        "kernel": "split_gemm_kernel (X build)",
                         "peak_source": "bf16_tflops_sustained of %s" % peak_kind,
                         "ms_per_launch": per_launch_ms, "executed_bf16_tflops": executed,
                         "executed_frac": (executed / peak) if executed else None},
-           "phases_ms_per_build_sample": {"pair": pair_ms / args.steps,
-                                          "x_gemm": gemm_ms / args.steps},
-           "e2e": {"value": None, "unit": UNIT,
-                   "reason": "the full build's host outputs (195 GB) exceed the GPU host's memory"}}
-
-    if not args.skip_accuracy:
-        rows = 128
-        log("large: accuracy on %d rows" % rows)
-        sub = strided_rows(p, rows)
-        out["accuracy"] = large_accuracy(cg, sub, args.slices)
-        out["accuracy"]["sample"] = ("%d of %d r1 rows spread over the grid; split (%d slices) vs "
-                                     "the plain FP64 form" % (rows, p.n_grid1, S))
-        log("large: plain FP64 rate")
-        out["plain_fp64"] = plain_rate_estimate(cg, p, (rows, 2 * rows))
-        out["speedup_vs_plain_fp64"] = value / out["plain_fp64"]["value_est"]
-    print(json.dumps(out), flush=True)
-    return 0
+           "phases_ms_per_build_sample": {"pair": pair_ms / steps, "x_gemm": gemm_ms / steps},
+           "e2e": {"value": None, "reason": "the full build's host outputs (195 GB) exceed the "
+                                            "GPU host's memory"}}
+    if with_accuracy:
+        log("large: accuracy vs the oracle")
+        out["accuracy"] = oracle_check(cg, p, 32, S)
+    return out
 
 
-def large_accuracy(cg, sub, n_slices):
-    """X and int_2e of the split form against the plain FP64 form on one r1 sample,
-    with int_2e compared in row blocks (one copy of it lives on the host)."""
+def oracle_check(cg, p, rows, n_slices):
+    """Both forms against the FP64 oracle on `rows` r1 points spread over the grid of
+    p, at its full n_ao and n_grid2, with the outputs left on the device: X in full,
+    48 rows of int_2e and int_2e times a random vector (oracle.x_rows,
+    int2e_rows, int2e_matvec form neither the whole P nor the n_ao^4 matrix)."""
     import torch
-    dev = torch.device("cuda", torch.cuda.current_device())
+    from oracle import oracle
+    sub = synth.r1_sample(p, rows)
     nA2 = sub.n_ao ** 2
-    ns = sub.n_grid1
-    dr = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in sub.arrays().items()}
-
-    def build(prec, X, I):
-        opt = cg.options(prec, n_slices if prec == cg.SPLIT_BF16 else None, sub.a_en, sub.a_ee,
-                         3, True, 0, None)
-        s = cg.cutc_int_ex(opt, ns, sub.n_grid2, sub.n_ao, sub.n_nuc, sub.size_bh,
-                           dr["r1"], dr["wr1"], dr["r2"], dr["wr2"], dr["rn"], dr["aos1"],
-                           dr["aos2"], dr["c_bh"], dr["m_bh"], dr["n_bh"], dr["o_bh"], X, I, None)
-        torch.cuda.synchronize(dev)
-        if s != cg.CUTC_OK:
-            raise cg.CutcError(s, cg.last_error())
-
-    X = torch.empty((3, ns, nA2), dtype=torch.float64, device=dev)
-    I = torch.empty((nA2, nA2), dtype=torch.float64, device=dev)
-    build(cg.SPLIT_BF16, X, I)
-    Xs = X.cpu().numpy()
-    Is = I.cpu().numpy()
-    cg.load().cutc_release()
-    build(cg.PLAIN_FP64, X, I)
-    from oracle.oracle import rel_err
-    ex = rel_err(Xs, X.cpu().numpy())
-    d2 = r2 = 0.0
-    dmax = rmax = 0.0
-    step = max(1, (1 << 30) // (8 * nA2))
-    for r0 in range(0, nA2, step):
-        ref = I[r0:r0 + step].cpu().numpy()
-        d = Is[r0:r0 + step] - ref
-        d2 += float(np.sum(d * d))
-        r2 += float(np.sum(ref * ref))
-        dmax = max(dmax, float(np.max(np.abs(d))))
-        rmax = max(rmax, float(np.max(np.abs(ref))))
-    del X, I, dr
-    torch.cuda.empty_cache()
-    cg.load().cutc_release()
-    return {"X_vs_fp64": ex, "int2e_vs_fp64": {"norm": (d2 / r2) ** 0.5 if r2 > 0 else d2 ** 0.5,
-                                               "max": dmax / rmax if rmax > 0 else dmax}}
+    rng = np.random.default_rng(2024)
+    sel = np.sort(rng.choice(nA2, min(nA2, 48), replace=False))
+    v = rng.standard_normal(nA2)
+    X4 = oracle.x_rows(sub)
+    S0, S = oracle.short_herm(sub), oracle.short_nonherm(sub)
+    I_sel = oracle.int2e_rows(sub, X4, sel, S0, S)
+    I_v = oracle.int2e_matvec(sub, X4, v, S0, S)
+    release_device()
+    res = {"sample": "%d of %d r1 rows spread over the grid, full n_ao and n_grid2; X in full, "
+                     "48 int_2e rows and int_2e v against the FP64 oracle"
+                     % (rows, p.n_grid1)}
+    buf = None
+    for name, prec in (("split", cg.SPLIT_BF16), ("plain", cg.PLAIN_FP64)):
+        X, I = cg.build_integrals_device(sub, prec, n_slices=n_slices if prec else None, out=buf)
+        buf = (X, I)
+        res[name] = {"X_vs_oracle": rel(X.cpu().numpy(), X4[:3]),
+                     "int2e_rows_vs_oracle": rel(I[torch.from_numpy(sel).to(I.device)].cpu().numpy(),
+                                                 I_sel),
+                     "int2e_v_vs_oracle": rel((I @ torch.from_numpy(v).to(I.device)).cpu().numpy(),
+                                              I_v)}
+        release_device()
+    del buf
+    release_device()
+    return res
 
 
+# ---------------------------------------------------------------------------
+# the Jastrow-parameter scan
+# ---------------------------------------------------------------------------
+def scan_sets(p, n, seed=5050):
+    rng = np.random.default_rng(seed)
+    return (rng.normal(0.0, 0.3, size=(n,) + p.c_bh.shape), rng.uniform(0.5, 2.0, n),
+            rng.uniform(0.5, 2.0, n))
+
+
+def scan_leg(cg, args, n_sets, with_accuracy, batch=8):
+    """The scan molecule with n_sets Jastrow parameter sets, `batch` sets per
+    cutc_int_scan call, outputs in reused pinned host memory."""
+    import torch
+    from oracle import oracle
+    p = synth.make_config("scan")
+    c_sets, a_en, a_ee = scan_sets(p, n_sets)
+    prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
+    batch = min(n_sets, batch)
+    nA2 = p.n_ao ** 2
+    Xo = torch.empty((batch, 3, p.n_grid1, nA2), dtype=torch.float64, pin_memory=True).numpy()
+    Io = torch.empty((batch, nA2, nA2), dtype=torch.float64, pin_memory=True).numpy()
+    cg.scan_integrals(p, c_sets[:batch], a_en[:batch], a_ee[:batch], prec, args.slices,
+                      out=(Xo, Io))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    launches = 0
+    for b0 in range(0, n_sets, batch):
+        sl = slice(b0, min(n_sets, b0 + batch))
+        k = sl.stop - sl.start
+        X, I, st = cg.scan_integrals(p, c_sets[sl], a_en[sl], a_ee[sl], prec, args.slices,
+                                     with_stats=True, out=(Xo[:k], Io[:k]))
+        launches += st["gpu_launches"]
+    elapsed = time.perf_counter() - t0
+    del Xo, Io
+    out = {"value": n_sets / elapsed, "unit": UNIT,
+           "workload": "scan: " + workload_desc("scan", p) + ", %d Jastrow parameter sets "
+                       "(c ~ N(0, 0.3), a_en, a_ee ~ U[0.5, 2]), %d sets per cutc_int_scan "
+                       "call, outputs in reused pinned host memory" % (n_sets, batch),
+           "precision": args.precision, "gpu_launches": launches,
+           "alg_tflops": n_sets * p.flops() / elapsed / 1e12}
+    release_device()
+    if with_accuracy:
+        rows, k = 64, 4
+        sub = synth.r1_sample(p, rows)
+        Xs, Is = cg.scan_integrals(sub, c_sets[:k], a_en[:k], a_ee[:k], cg.SPLIT_BF16, args.slices)
+        Xp, Ip = cg.scan_integrals(sub, c_sets[:k], a_en[:k], a_ee[:k], cg.PLAIN_FP64)
+        worst = {"split": {"X": 0.0, "int2e": 0.0}, "plain": {"X": 0.0, "int2e": 0.0}}
+        for s in range(k):
+            q = dataclasses.replace(sub, c_bh=np.ascontiguousarray(c_sets[s]), a_en=float(a_en[s]),
+                                    a_ee=float(a_ee[s]))
+            Xr, Ir = oracle.cutc_int(q)
+            for name, Xg, Ig in (("split", Xs[s], Is[s]), ("plain", Xp[s], Ip[s])):
+                ex, ei = rel(Xg, Xr), rel(Ig, Ir)
+                worst[name]["X"] = max(worst[name]["X"], ex["norm"], ex["max"])
+                worst[name]["int2e"] = max(worst[name]["int2e"], ei["norm"], ei["max"])
+        out["accuracy"] = {"worst_vs_oracle": worst,
+                           "sample": "%d of %d r1 rows, the first %d sets; the worst of the "
+                                     "normwise and max-abs/max relative errors against the "
+                                     "FP64 oracle" % (rows, p.n_grid1, k)}
+        release_device()
+    return out
+
+
+# ---------------------------------------------------------------------------
+# the serving stream
+# ---------------------------------------------------------------------------
 def serving_requests(n, max_ao, seed=4004):
     """The serving stream: molecules of 2-20 nuclei, n_ao uniform in [10, max_ao],
     n_grid1 = 1000 n_nuc, n_grid2 = 4000 n_nuc; 30% repeat an earlier molecule with
     Jastrow coefficients perturbed by a 10% Gaussian.  Molecules carry their basis,
     not AO arrays: the server evaluates the AOs on the GPU."""
-    import dataclasses
     rng = np.random.default_rng(seed)
     mols, reqs = [], []
     for i in range(n):
@@ -682,25 +782,18 @@ def output_bytes(p):
     return 8 * (3 * p.n_grid1 * p.n_ao ** 2 + p.n_ao ** 4)
 
 
-def run_serving(args):
-    """Poisson arrivals into the continuous-batching server; p50/p99 latency and builds/s.
-
-    The host holds at most --host-gb of request outputs at a time (X and int_2e of
-    an n_ao = 250 request are 61 GB): past that, the stream waits for the oldest
-    request before submitting the next, and the time it waited is reported."""
-    import cutc_gb300 as cg
-    import torch
-    torch.cuda.set_device(0)
-    reqs = serving_requests(args.requests, args.max_ao)
-    log("serving: %d requests generated" % len(reqs))
-    prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
+def serving_stream(cg, reqs, rate, prec, n_slices, slots, host_gb):
+    """Poisson arrivals into the continuous-batching server.  The host holds at most
+    host_gb of request outputs at a time (X and int_2e of an n_ao = 250 request are
+    61 GB): past that, the stream waits for the oldest request before submitting the
+    next, and the time it waited is reported."""
     rng = np.random.default_rng(7)
-    gaps = rng.exponential(1.0 / args.rate, size=len(reqs))
-    budget = args.host_gb * 1e9
+    gaps = rng.exponential(1.0 / rate, size=len(reqs))
+    budget = host_gb * 1e9
     lat = []
     held = 0.0
     t_blocked = 0.0
-    with cg.Server(n_slots=args.slots) as srv:
+    with cg.Server(n_slots=slots) as srv:
         t0 = time.perf_counter()
         tickets = []  # (ticket, output bytes)
         t_next = t0
@@ -715,119 +808,208 @@ def run_serving(args):
                 lat.append(srv.wait(t)[2])
                 held -= b
             t_blocked += time.perf_counter() - tb
-            tickets.append((srv.submit(p, key, prec, args.slices, aos_from_basis=True), need))
+            tickets.append((srv.submit(p, key, prec, n_slices, aos_from_basis=True), need))
             held += need
         for t, _ in tickets:
             lat.append(srv.wait(t)[2])
         elapsed = time.perf_counter() - t0
         st = srv.stats()
     flops = sum(p.flops() for _, p in reqs)
-    accuracy = None
-    if not args.skip_accuracy:
-        accuracy = serving_accuracy(cg, reqs, args.slices)
-    line = {"metric": "TC integral builds/s and latency, serving stream", "value": len(reqs) / elapsed,
-            "unit": "builds/s", "n_gpus": 1, "higher_is_better": True,
-            "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
-            "config": {"workload": "serving: %d requests, Poisson arrivals at %.1f/s, 2-20 nuclei, "
-                                   "n_ao in [10, %d], n_grid1 = 1000 n_nuc, n_grid2 = 4000 n_nuc, "
-                                   "30%% repeats with perturbed Jastrow coefficients, AOs evaluated "
-                                   "on the GPU from each request's basis"
-                                   % (len(reqs), args.rate, args.max_ao),
-                       "slots": args.slots, "precision": args.precision,
-                       "host_output_budget_gb": args.host_gb},
+    return {"value": len(reqs) / elapsed, "unit": UNIT,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "arrivals_held_back_s": t_blocked,
-            "server": st, "alg_tflops": flops / elapsed / 1e12, "accuracy": accuracy}
-    print(json.dumps(line), flush=True)
-    return 0
+            "max_ms": float(np.max(lat)), "arrivals_held_back_s": t_blocked,
+            "server": st, "alg_tflops": flops / elapsed / 1e12}
 
 
-def serving_accuracy(cg, reqs, n_slices, rows=128, max_ao=200):
-    """Split vs plain FP64 for three molecules of the stream (smallest, median and
-    largest n_ao up to max_ao, so that int_2e stays a few GB), on `rows` r1 points
-    spread over each grid, AOs from the basis as in the stream."""
-    import dataclasses
-    from oracle.oracle import rel_err
-    mols = {}
-    for key, p in reqs:
-        if p.n_ao <= max_ao and key not in mols:
-            mols[key] = p
-    ps = sorted(mols.values(), key=lambda q: q.n_ao)
-    pick = [ps[0], ps[len(ps) // 2], ps[-1]] if len(ps) >= 3 else ps
-    out = []
-    for p in pick:
-        idx = np.unique(np.linspace(0, p.n_grid1 - 1, min(rows, p.n_grid1)).round().astype(np.int64))
-        sub = dataclasses.replace(p, r1=np.ascontiguousarray(p.r1[idx]),
-                                  wr1=np.ascontiguousarray(p.wr1[idx]))
-        Xs, Is = cg.build_integrals(sub, cg.SPLIT_BF16, n_slices=n_slices, aos_from_basis=True)
-        Xp, Ip = cg.build_integrals(sub, cg.PLAIN_FP64, aos_from_basis=True)
-        out.append({"n_nuc": p.n_nuc, "n_ao": p.n_ao, "n_grid2": p.n_grid2, "r1_rows": len(idx),
-                    "X_vs_fp64": rel_err(Xs, Xp), "int2e_vs_fp64": rel_err(Is, Ip)})
-        del Xs, Is, Xp, Ip
+def serving_leg(cg, args, n, rate, max_ao, with_accuracy, plain_fp64_tflops):
+    """The first n requests of the serving stream (BASELINE rate and n_ao range) in
+    the split form, p50/p99 latency and builds/s; the plain FP64 form's rate on the
+    same requests from its measured FP64 contraction rate; one molecule of the
+    prefix against the oracle in both forms."""
+    reqs = serving_requests(n, max_ao)
+    out = serving_stream(cg, reqs, rate, cg.SPLIT_BF16, args.slices, 4, 48.0)
+    out["workload"] = ("serving: the first %d requests of the 256-request stream, Poisson "
+                       "arrivals at %.1f/s, 2-20 nuclei, n_ao in [10, %d], n_grid1 = 1000 n_nuc, "
+                       "n_grid2 = 4000 n_nuc, 30%% repeats with perturbed Jastrow coefficients, "
+                       "AOs evaluated on the GPU from each request's basis, 4 slots"
+                       % (n, rate, max_ao))
+    out["precision"] = "split"
+    if plain_fp64_tflops:
+        # the plain form's dominant cost is its FP64 contractions: packed X (4 nA(nA+1) n1 n2
+        # flops) and int_2e (about 4 nA^4 n1 with the packed pairs)
+        secs = [(4.0 * q.n_ao * (q.n_ao + 1) * q.n_grid1 * q.n_grid2 + 4.0 * q.n_ao ** 4 * q.n_grid1)
+                / (plain_fp64_tflops * 1e12) for _, q in reqs]
+        out["plain_projection"] = {
+            "builds_per_s": len(reqs) / sum(secs), "mean_s_per_request": float(np.mean(secs)),
+            "basis": "each request's packed FP64 contraction flops at the plain form's measured "
+                     "X-contraction rate (%.3f TF/s); the stream's arrival rate exceeds this "
+                     "service rate, so its latency grows without bound" % plain_fp64_tflops}
+    if with_accuracy:
+        ps = sorted({k: q for k, q in reqs if q.n_ao <= 200}.values(), key=lambda q: q.n_ao)
+        if ps:
+            q = ps[-1]
+            q = dataclasses.replace(q, aos1=synth.eval_aos(q.shells, q.r1),
+                                    aos2=synth.eval_aos(q.shells, q.r2))
+            out["accuracy"] = oracle_check(cg, q, 32, args.slices)
+            out["accuracy"]["molecule"] = {"n_nuc": q.n_nuc, "n_ao": q.n_ao, "n_grid2": q.n_grid2}
+    release_device()
     return out
 
 
-def run_scan(args):
-    """Batched Jastrow-parameter scan: one molecule, n_sets parameter sets."""
-    import dataclasses
-    import cutc_gb300 as cg
+# ---------------------------------------------------------------------------
+# the rival: cuBLAS's own FP64 emulation on the split contraction's operands
+# ---------------------------------------------------------------------------
+class Cublas:
+    """The handful of cuBLAS calls the rival leg needs, through ctypes (cuBLAS is
+    not linked into this library)."""
+    OP_N, OP_T = 0, 1
+    FP64_EMULATED_FIXEDPOINT_MATH = 8  # cublasMath_t
+    EMULATION_STRATEGY_EAGER = 2       # cublasEmulationStrategy_t
+    MANTISSA_DYNAMIC, MANTISSA_FIXED = 0, 1  # cudaEmulationMantissaControl
+
+    def __init__(self):
+        self.L = None
+        for name in ("libcublas.so.13", "/usr/local/cuda/lib64/libcublas.so.13",
+                     "/usr/local/cuda/lib64/libcublas.so"):
+            try:
+                self.L = ctypes.CDLL(name)
+                break
+            except OSError:
+                continue
+        if self.L is None:
+            raise RuntimeError("libcublas not found")
+        L, vp, i = self.L, ctypes.c_void_p, ctypes.c_int
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.cublasCreate_v2.argtypes = [ctypes.POINTER(vp)]
+        L.cublasDestroy_v2.argtypes = [vp]
+        L.cublasSetStream_v2.argtypes = [vp, vp]
+        L.cublasSetMathMode.argtypes = [vp, i]
+        L.cublasSetWorkspace_v2.argtypes = [vp, vp, ctypes.c_size_t]
+        L.cublasDgemm_v2.argtypes = [vp, i, i, i, i, i, dp, vp, i, vp, i, dp, vp, i]
+        for f in ("cublasSetEmulationStrategy", "cublasSetFixedPointEmulationMantissaControl",
+                  "cublasSetFixedPointEmulationMaxMantissaBitCount"):
+            getattr(L, f).argtypes = [vp, i]
+        self.h = vp()
+        self._check(L.cublasCreate_v2(ctypes.byref(self.h)), "cublasCreate")
+
+    @staticmethod
+    def _check(s, what):
+        if s != 0:
+            raise RuntimeError("%s: cuBLAS status %d" % (what, s))
+
+    def configure(self, stream, workspace, emulated, mantissa_bits=None):
+        L = self.L
+        self._check(L.cublasSetStream_v2(self.h, stream), "cublasSetStream")
+        self._check(L.cublasSetWorkspace_v2(self.h, workspace.data_ptr(), workspace.numel()),
+                    "cublasSetWorkspace")
+        if not emulated:
+            self._check(L.cublasSetMathMode(self.h, 0), "cublasSetMathMode")
+            return
+        self._check(L.cublasSetMathMode(self.h, self.FP64_EMULATED_FIXEDPOINT_MATH),
+                    "cublasSetMathMode(FP64_EMULATED_FIXEDPOINT)")
+        self._check(L.cublasSetEmulationStrategy(self.h, self.EMULATION_STRATEGY_EAGER),
+                    "cublasSetEmulationStrategy(EAGER)")
+        if mantissa_bits is None:
+            self._check(L.cublasSetFixedPointEmulationMantissaControl(self.h, self.MANTISSA_DYNAMIC),
+                        "mantissa control DYNAMIC")
+        else:
+            self._check(L.cublasSetFixedPointEmulationMantissaControl(self.h, self.MANTISSA_FIXED),
+                        "mantissa control FIXED")
+            self._check(L.cublasSetFixedPointEmulationMaxMantissaBitCount(self.h, mantissa_bits),
+                        "max mantissa bits")
+
+    def gemm_nt(self, M, N, K, A, B, C):
+        """C (M x N, column-major) = A B^T with A (M x K) and B (N x K) row-major."""
+        one, zero = ctypes.c_double(1.0), ctypes.c_double(0.0)
+        self._check(self.L.cublasDgemm_v2(self.h, self.OP_T, self.OP_N, M, N, K, ctypes.byref(one),
+                                          A.data_ptr(), K, B.data_ptr(), K, ctypes.byref(zero),
+                                          C.data_ptr(), M), "cublasDgemm")
+
+    def close(self):
+        self.L.cublasDestroy_v2(self.h)
+
+
+def rival_shapes(p, dr, Xd, n_cols):
+    """The split contraction's real operands on the medium molecule, as FP64
+    row-major device tensors: the X build (A = packed pair products P, B = rows of
+    the pair-term planes G of n_cols / 4 r1 points, K = n_grid2) and an int_2e
+    contraction (A = packed X_0 over all r1 points, B = n_cols packed S0 rows,
+    K = n_grid1)."""
     import torch
-    from oracle.oracle import rel_err
-    torch.cuda.set_device(0)
-    p = synth.make_config("scan")
-    rng = np.random.default_rng(5050)
-    ns = args.sets
-    c_sets = rng.normal(0.0, 0.3, size=(ns,) + p.c_bh.shape)
-    a_en = rng.uniform(0.5, 2.0, ns)
-    a_ee = rng.uniform(0.5, 2.0, ns)
-    prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
-    batch = min(ns, args.scan_batch)
-    # the outputs of one call live in pinned host memory reused by every call, as a
-    # scanning caller would keep them
-    nA2 = p.n_ao ** 2
-    Xo = torch.empty((batch, 3, p.n_grid1, nA2), dtype=torch.float64, pin_memory=True).numpy()
-    Io = torch.empty((batch, nA2, nA2), dtype=torch.float64, pin_memory=True).numpy()
-    log("scan: warm-up")
-    cg.scan_integrals(p, c_sets[:batch], a_en[:batch], a_ee[:batch], prec, args.slices,
-                      out=(Xo, Io))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    launches = 0
-    for b0 in range(0, ns, batch):
-        sl = slice(b0, min(ns, b0 + batch))
-        k = sl.stop - sl.start
-        X, I, st = cg.scan_integrals(p, c_sets[sl], a_en[sl], a_ee[sl], prec, args.slices,
-                                     with_stats=True, out=(Xo[:k], Io[:k]))
-        launches += st["gpu_launches"]
-    elapsed = time.perf_counter() - t0
-    log("scan: %.3f sets/s; accuracy sample" % (ns / elapsed))
-    rows = 256
-    i0 = (p.n_grid1 // 2) // 64 * 64
-    sub = dataclasses.replace(p, r1=np.ascontiguousarray(p.r1[i0:i0 + rows]),
-                              wr1=np.ascontiguousarray(p.wr1[i0:i0 + rows]),
-                              aos1=np.ascontiguousarray(p.aos1[:, :, i0:i0 + rows]))
-    Xs, Is = cg.scan_integrals(sub, c_sets, a_en, a_ee, prec, args.slices)
-    Xp, Ip = cg.scan_integrals(sub, c_sets, a_en, a_ee, cg.PLAIN_FP64)
-    ex = [rel_err(Xs[k], Xp[k]) for k in range(ns)]
-    ei = [rel_err(Is[k], Ip[k]) for k in range(ns)]
-    line = {"metric": "TC integral builds/s, Jastrow-parameter scan", "value": ns / elapsed,
-            "unit": "builds/s", "n_gpus": 1, "higher_is_better": True,
-            "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
-            "config": {"workload": "scan: " + workload_desc("scan", p) + ", %d Jastrow parameter "
-                                   "sets (c ~ N(0, 0.3), a_en, a_ee ~ U[0.5, 2]), %d sets per "
-                                   "cutc_int_scan call, outputs in reused pinned host memory"
-                                   % (ns, batch),
-                       "precision": args.precision},
-            "gpu_launches": launches,
-            "alg_tflops": ns * p.flops() / elapsed / 1e12,
-            "accuracy": {"X_vs_fp64_max_over_sets": max(e["norm"] for e in ex),
-                         "X_vs_fp64_maxabs_max_over_sets": max(e["max"] for e in ex),
-                         "int2e_vs_fp64_max_over_sets": max(e["norm"] for e in ei),
-                         "int2e_vs_fp64_maxabs_max_over_sets": max(e["max"] for e in ei),
-                         "sample": "%d of %d r1 rows, every set; split vs the plain FP64 form"
-                                   % (rows, p.n_grid1)}}
-    print(json.dumps(line), flush=True)
-    return 0
+    import cutc_gb300 as cg
+    dev = Xd.device
+    nA = p.n_ao
+    a_idx, b_idx = np.tril_indices(nA)  # packed pairs a >= b
+    order = np.lexsort((a_idx, b_idx))  # column by column, as the library packs them
+    a_t = torch.from_numpy(a_idx[order]).to(dev)
+    b_t = torch.from_numpy(b_idx[order]).to(dev)
+    chi2 = dr["aos2"][0]  # (nA, n2): value component
+    P = (dr["wr2"][None, :] * chi2[a_t]) * chi2[b_t]
+    nr1 = n_cols // 4
+    G = torch.empty((4, nr1, p.n_grid2), dtype=torch.float64, device=dev)
+    s = cg.jast_bh_device(dr["r1"], dr["r2"], dr["rn"], dr["c_bh"], dr["m_bh"], dr["n_bh"],
+                          dr["o_bh"], G, i0=0, n1b=nr1, a_en=p.a_en, a_ee=p.a_ee)
+    if s != cg.CUTC_OK:
+        raise cg.CutcError(s, cg.last_error())
+    Bx = G.reshape(4 * nr1, p.n_grid2)
+    X0 = Xd[0][:, a_t * nA + b_t].T.contiguous()  # (np, n1)
+    chi1 = dr["aos1"][0]  # (nA, n1)
+    sel = torch.arange(0, min(n_cols, a_t.numel()), device=dev)
+    S0 = (dr["wr1"][None, :] * chi1[a_t[sel]]) * chi1[b_t[sel]]
+    return [("X build", P, Bx), ("int_2e (N contraction shape)", X0, S0.contiguous())]
+
+
+def rival_leg(cg, p, dr, Xd, n_slices, n_cols=2048, bits=(None, 40)):
+    """cuBLAS FP64 DGEMM, this library's FP64 DMMA GEMM, cuBLAS with FP64
+    fixed-point emulation (dynamic and fixed mantissa bits) and the split
+    contraction on the same operands; errors against the cuBLAS FP64 result."""
+    import torch
+    dev = Xd.device
+    out = {"note": "each call's device time (CUDA events) includes the slicing of both operands "
+                   "for the emulated and split forms; errors are normwise and max-abs/max "
+                   "against cuBLAS FP64 DGEMM on the same operands"}
+    cb = Cublas()
+    ws = torch.empty(4 << 30, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    try:
+        for name, A, B in rival_shapes(p, dr, Xd, n_cols):
+            M, K = A.shape
+            N = B.shape[0]
+            flops = 2.0 * M * N * K
+            rec = {"M": M, "N": N, "K": K}
+            C_ref = torch.empty((N, M), dtype=torch.float64, device=dev)
+            cb.configure(stream, ws, False)
+            cb.gemm_nt(M, N, K, A, B, C_ref)  # warm-up
+            ms = cuda_ms(lambda: cb.gemm_nt(M, N, K, A, B, C_ref))
+            rec["cublas_fp64"] = {"ms": ms, "fp64_tflops": flops / ms / 1e9}
+            C = torch.empty_like(C_ref)
+            cg.fp64_gemm_device(True, M, N, K, 1.0, A, K, B, K, 0.0, C, M)
+            ms = cuda_ms(lambda: cg.fp64_gemm_device(True, M, N, K, 1.0, A, K, B, K, 0.0, C, M))
+            rec["ours_fp64_dmma"] = {"ms": ms, "fp64_tflops": flops / ms / 1e9,
+                                     "err": rel(C.cpu().numpy(), C_ref.cpu().numpy())}
+            ref_h = C_ref.cpu().numpy()
+            for b in bits:
+                key = "cublas_emulated_%s" % ("dynamic" if b is None else "fixed%d" % b)
+                try:
+                    cb.configure(stream, ws, True, b)
+                    cb.gemm_nt(M, N, K, A, B, C)
+                    ms = cuda_ms(lambda: cb.gemm_nt(M, N, K, A, B, C))
+                    rec[key] = {"ms": ms, "fp64_equiv_tflops": flops / ms / 1e9,
+                                "err": rel(C.cpu().numpy(), ref_h)}
+                except Exception as e:  # noqa: BLE001
+                    rec[key] = {"error": repr(e)[:200]}
+            cg.split_gemm_device(A, B, C, n_slices=n_slices)
+            ms = cuda_ms(lambda: cg.split_gemm_device(A, B, C, n_slices=n_slices))
+            rec["ours_split_%d" % n_slices] = {"ms": ms, "fp64_equiv_tflops": flops / ms / 1e9,
+                                               "err": rel(C.cpu().numpy(), ref_h)}
+            out[name] = rec
+            log("rival %s: %s" % (name, json.dumps(rec)))
+            del C, C_ref, A, B
+    finally:
+        cb.close()
+        del ws
+        release_device()
+    return out
 
 
 def traffic_per_launch(args, p, launches):
@@ -847,6 +1029,132 @@ def traffic_per_launch(args, p, launches):
         return None
 
 
+# ---------------------------------------------------------------------------
+# single-kernel micro-benchmarks (the cases of the committed ncu summaries)
+# ---------------------------------------------------------------------------
+def run_kernel(args):
+    import torch
+    import cutc_gb300 as cg
+    torch.cuda.set_device(0)
+    k = args.kernel
+    if k in ("split_gemm", "fp64_gemm"):
+        # C = A B^T on seeded FP64 operands shaped like the X build of cutc_int
+        # (m packed AO pairs, n = 4 x r1 points, k = r2 points)
+        g = torch.Generator(device="cuda").manual_seed(1234)
+        A = torch.randn((args.m, args.k), dtype=torch.float64, device="cuda", generator=g)
+        B = torch.randn((args.n, args.k), dtype=torch.float64, device="cuda", generator=g)
+        C = torch.empty((args.n, args.m), dtype=torch.float64, device="cuda")
+        if k == "split_gemm":
+            call = lambda: cg.split_gemm_device(A, B, C, n_slices=args.slices)
+        else:
+            call = lambda: cg.fp64_gemm_device(True, args.m, args.n, args.k, 1.0, A, args.k, B,
+                                               args.k, 0.0, C, args.m)
+        times = [cuda_ms(call) for _ in range(args.reps)]
+        alg = 2.0 * args.m * args.n * args.k
+        ms = min(times)
+        rec = {"kernel": k, "m": args.m, "n": args.n, "k": args.k, "ms_call": ms,
+               "fp64_equiv_tflops": alg / ms / 1e9}
+        if k == "split_gemm":
+            S = args.slices
+            rec.update(slices=S, bf16_tflops_executed=alg * S * (S + 1) / 2 / ms / 1e9,
+                       note="call time includes slicing both operands")
+        print(json.dumps(rec))
+    elif k == "pair":
+        # a molecule with the medium workload's nuclei and Jastrow terms but few AOs (the
+        # pair terms do not depend on n_ao), so the device holds a few GB
+        p = synth.make_problem(n_nuc=args.n_nuc, n_ao=40, n_grid1=args.n1, n_grid2=args.n2,
+                               size_bh=args.terms, seed=2002, box=6.0)
+        pair_ms = []
+        for _ in range(args.reps):
+            _, _, st = cg.build_integrals(p, cg.SPLIT_BF16, with_stats=True)
+            pair_ms.append(st["ms_pair"])
+        ms = min(pair_ms)
+        print(json.dumps({"kernel": k, "n_nuc": args.n_nuc, "terms_per_nucleus": args.terms,
+                          "n1": args.n1, "n2": args.n2, "pair_ms": ms,
+                          "pairs_per_s": args.n1 * args.n2 / ms * 1e3,
+                          "pair_nucleus_evals_per_s": args.n1 * args.n2 * args.n_nuc / ms * 1e3}))
+    elif k == "plain_build":
+        # the medium molecule in the plain FP64 form on `rows` r1 points spread over its grid
+        p = synth.make_config("medium")
+        sub = synth.r1_sample(p, args.rows)
+        for _ in range(args.reps):
+            _, _, st = cg.build_integrals(sub, cg.PLAIN_FP64, with_stats=True)
+        np_ = p.n_ao * (p.n_ao + 1) // 2
+        flops_x = 2.0 * np_ * 4 * args.rows * p.n_grid2
+        print(json.dumps({"kernel": k, "rows": args.rows, "ms_total": st["ms_total"],
+                          "ms_x_gemm": st["ms_x_gemm"], "ms_int2e": st["ms_int2e"],
+                          "ms_pair": st["ms_pair"],
+                          "x_gemm_fp64_tflops": flops_x / st["ms_x_gemm"] / 1e9}))
+    elif k == "rival":
+        p = synth.make_config("medium")
+        dev = torch.device("cuda", 0)
+        dr = {kk: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for kk, v in p.arrays().items()}
+        Xd = torch.empty((3, p.n_grid1, p.n_ao ** 2), dtype=torch.float64, device=dev)
+        cg.build_integrals_device(p, cg.SPLIT_BF16, n_slices=args.slices,
+                                  out=(Xd, torch.empty((p.n_ao ** 2,) * 2, dtype=torch.float64,
+                                                       device=dev)))
+        bits = [None if b == "dynamic" else int(b) for b in args.bits]
+        print(json.dumps(rival_leg(cg, p, dr, Xd, args.slices, args.n, bits)))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# stand-alone legs
+# ---------------------------------------------------------------------------
+def run_large_cli(args):
+    import torch
+    import cutc_gb300 as cg
+    torch.cuda.set_device(0)
+    leg = large_leg(cg, args, args.warmup, args.steps, not args.skip_accuracy,
+                    (args.r1_sample // 2, args.r1_sample))
+    S = args.slices
+    out = {"metric": METRIC, "value": leg["value"], "unit": UNIT, "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": leg["ms_per_build"],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16" if args.precision == "split" else "f64", "data": "synthetic",
+           "config": {"workload": leg["workload"], "precision": args.precision, "n_slices": S,
+                      "projection": leg["projection"], "parallelism": "1 GPU",
+                      "l2": "inputs larger than L2: P slices alone are %.0f GB"
+                            % (2 * S * 300 * 301 / 2 * 200000 / 1e9)}}
+    out.update({k: v for k, v in leg.items() if k not in out and k not in ("workload",)})
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_serving_cli(args):
+    import cutc_gb300 as cg
+    import torch
+    torch.cuda.set_device(0)
+    reqs = serving_requests(args.requests, args.max_ao)
+    log("serving: %d requests generated" % len(reqs))
+    prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
+    line = serving_stream(cg, reqs, args.rate, prec, args.slices, args.slots, args.host_gb)
+    line.update({"metric": "TC integral builds/s and latency, serving stream", "n_gpus": 1,
+                 "higher_is_better": True,
+                 "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
+                 "config": {"workload": "serving: %d requests, Poisson arrivals at %.1f/s, 2-20 "
+                                        "nuclei, n_ao in [10, %d], n_grid1 = 1000 n_nuc, n_grid2 = "
+                                        "4000 n_nuc, 30%% repeats with perturbed Jastrow "
+                                        "coefficients, AOs evaluated on the GPU from each "
+                                        "request's basis" % (len(reqs), args.rate, args.max_ao),
+                            "slots": args.slots, "precision": args.precision,
+                            "host_output_budget_gb": args.host_gb}})
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_scan_cli(args):
+    import cutc_gb300 as cg
+    import torch
+    torch.cuda.set_device(0)
+    leg = scan_leg(cg, args, args.sets, not args.skip_accuracy, args.scan_batch)
+    leg.update({"metric": "TC integral builds/s, Jastrow-parameter scan", "n_gpus": 1,
+                "higher_is_better": True, "data": "synthetic",
+                "dtype": "bf16" if args.precision == "split" else "f64"})
+    print(json.dumps(leg), flush=True)
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -860,10 +1168,16 @@ def main(argv=None):
                     help="max K per tensor-core launch (0 = library default)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--skip-rival", action="store_true")
+    ap.add_argument("--skip-large", action="store_true")
+    ap.add_argument("--skip-scan", action="store_true")
+    ap.add_argument("--skip-serving", action="store_true")
+    ap.add_argument("--main-only", action="store_true",
+                    help="the medium line alone: skip the CPU, accuracy and extra legs")
     ap.add_argument("--serving", action="store_true", help="run the serving stream instead")
     ap.add_argument("--requests", type=int, default=256)
-    ap.add_argument("--rate", type=float, default=8.0, help="serving arrivals per second")
-    ap.add_argument("--max-ao", type=int, default=120)
+    ap.add_argument("--rate", type=float, default=1.0, help="serving arrivals per second")
+    ap.add_argument("--max-ao", type=int, default=250)
     ap.add_argument("--slots", type=int, default=4)
     ap.add_argument("--host-gb", type=float, default=48.0,
                     help="serving: host memory for outputs of requests in flight")
@@ -872,15 +1186,33 @@ def main(argv=None):
     ap.add_argument("--scan-batch", type=int, default=8)
     ap.add_argument("--r1-sample", type=int, default=6000,
                     help="large workload: r1 rows of the bigger of the two timed samples")
+    ap.add_argument("--kernel", choices=["split_gemm", "fp64_gemm", "pair", "plain_build", "rival"],
+                    help="run one kernel's micro-benchmark instead")
+    ap.add_argument("--m", type=int, default=7260)
+    ap.add_argument("--n", type=int, default=2048)
+    ap.add_argument("--k", type=int, default=16384)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--rows", type=int, default=256)
+    ap.add_argument("--n-nuc", type=int, default=10)
+    ap.add_argument("--terms", type=int, default=13)
+    ap.add_argument("--n1", type=int, default=1024)
+    ap.add_argument("--n2", type=int, default=80000)
+    ap.add_argument("--bits", nargs="+", default=["dynamic", "40"],
+                    help="rival: mantissa settings of cuBLAS's FP64 emulation")
     args = ap.parse_args(argv)
+    if args.main_only:
+        args.skip_cpu = args.skip_accuracy = args.skip_rival = True
+        args.skip_large = args.skip_scan = args.skip_serving = True
+    if args.kernel:
+        return run_kernel(args)
     if args.serving:
-        return run_serving(args)
+        return run_serving_cli(args)
     if args.scan:
-        return run_scan(args)
+        return run_scan_cli(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.config == "large":
-        return run_large(args)
+        return run_large_cli(args)
     return run_ours(args)
 
 

@@ -30,7 +30,8 @@ SPLIT_BF16 = 1
 
 # every symbol include/cutc_int.h declares
 EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_int_scan", "cutc_default_options", "cutc_jast_bh_dev",
-           "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_validate_launch_dims",
+           "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_fp64_gemm_dev",
+           "cutc_validate_launch_dims",
            "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
            "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy",
            "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos",
@@ -156,6 +157,10 @@ def load(path: str = LIB_PATH):
     L.cutc_jast_bh_dev_noalloc.restype = i
     L.cutc_split_gemm_dev.argtypes = [i, i, i, ctypes.c_longlong, vp, vp, vp, ctypes.c_longlong]
     L.cutc_split_gemm_dev.restype = i
+    ll = ctypes.c_longlong
+    L.cutc_fp64_gemm_dev.argtypes = [i, i, i, ll, ctypes.c_double, vp, ll, ll, vp, ll, ll,
+                                     ctypes.c_double, vp, ll, ll, i]
+    L.cutc_fp64_gemm_dev.restype = i
     L.cutc_validate_launch_dims.argtypes = [i] * 6
     L.cutc_validate_launch_dims.restype = i
     L.cutc_last_error.argtypes = []
@@ -280,6 +285,33 @@ def build_integrals(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
     s = cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
                     p.r1, p.wr1, p.r2, p.wr2, p.rn, aos1, aos2,
                     p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I, st)
+    if s != CUTC_OK:
+        raise CutcError(s, last_error())
+    return (X, I, st.as_dict()) if with_stats else (X, I)
+
+
+def build_integrals_device(p, precision=PLAIN_FP64, n_slices=None, x_components=3,
+                           out=None, with_stats=False):
+    """Device-resident build on a synth.Problem: the molecule arrays are copied to
+    the current CUDA device (torch tensors) and X, int_2e stay there, for outputs
+    too large for the host.  out=(X, I) reuses float64 device tensors of shapes
+    (x_components, n1, nA^2) and (nA^2, nA^2).  Returns (X, I[, stats])."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in p.arrays().items()}
+    nA2 = p.n_ao ** 2
+    if out is None:
+        X = torch.empty((x_components, p.n_grid1, nA2), dtype=torch.float64, device=dev)
+        I = torch.empty((nA2, nA2), dtype=torch.float64, device=dev)
+    else:
+        X, I = out
+    st = Stats()
+    opt = options(precision, n_slices, p.a_en, p.a_ee, x_components, True, 0,
+                  torch.cuda.current_stream(dev).cuda_stream)
+    s = cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                    d["r1"], d["wr1"], d["r2"], d["wr2"], d["rn"], d["aos1"], d["aos2"],
+                    d["c_bh"], d["m_bh"], d["n_bh"], d["o_bh"], X, I, st)
+    torch.cuda.synchronize(dev)
     if s != CUTC_OK:
         raise CutcError(s, last_error())
     return (X, I, st.as_dict()) if with_stats else (X, I)
@@ -414,6 +446,17 @@ def jast_bh_device_noalloc(r1, r2, rn, c_bh, m_bh, n_bh, o_bh, G, i0=0, n1b=None
     return L.cutc_jast_bh_dev_noalloc(i0, n1b, n1, r2.shape[0], rn.shape[0], c_bh.shape[1],
                                       _vp(r1), _vp(r2), _vp(rn), _vp(c_bh), _vp(m_bh), _vp(n_bh),
                                       _vp(o_bh), a_en, a_ee, _vp(G), stream)
+
+
+def fp64_gemm_device(a_kmajor, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, stride_a=0,
+                     stride_b=0, stride_c=0, batch=1):
+    """The plain form's FP64 DMMA GEMM on device tensors, with cuBLAS's
+    column-major argument meaning (cutc_fp64_gemm_dev); raises on a status."""
+    s = load().cutc_fp64_gemm_dev(int(bool(a_kmajor)), M, N, K, alpha, _vp(A), lda, stride_a,
+                                  _vp(B), ldb, stride_b, beta, _vp(C), ldc, stride_c, batch)
+    if s != CUTC_OK:
+        raise CutcError(s, last_error())
+    return C
 
 
 def split_gemm_device(A, B, C=None, n_slices=5):

@@ -84,7 +84,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 print(o)
     objs = [j[-1] for j in jobs]
     tmp = LIB + ".tmp%d" % os.getpid()
-    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcublas",
+    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs,
           "-Xlinker", "-rpath," + os.path.join(home, "lib64"),
           "-Xlinker", "--no-undefined"])
     os.replace(tmp, LIB)

@@ -3,7 +3,7 @@
 // Counterpart of the reference's host drivers src/cutc_int.c:15-243,
 // src/build_int2_grad1_u12_ao.cu:9-347 and src/build_int_2e_ao.cu:11-145,
 // redesigned:
-//   * one engine per device with its own stream, cuBLAS handle and a
+//   * one engine per device with its own streams and a
 //     grow-only workspace (no cudaMalloc/cudaFree per call, no
 //     cudaDeviceSynchronize between steps: everything is stream-ordered);
 //   * r1 is tiled by a byte budget in 64-bit arithmetic (the reference sizes
@@ -13,8 +13,6 @@
 //   * X is accumulated per r1 tile with beta = 0, so r1 tiling is exact (the
 //     reference keeps beta = 1 across r1 passes, src/build_int2_grad1_u12_ao.cu:166);
 //   * errors are returned as status codes, never exit().
-#include <cublas_v2.h>
-
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -28,6 +26,7 @@
 
 #include "aos.cuh"
 #include "common.cuh"
+#include "dgemm.cuh"
 #include "engine.cuh"
 #include "pair.cuh"
 #include "products.cuh"
@@ -53,16 +52,6 @@ namespace cutc {
 static std::atomic<long> g_launches{0};
 void note_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
-
-#define CUBLAS_TRY(expr)                                                              \
-    do {                                                                              \
-        cublasStatus_t cutc_blas_ = (expr);                                           \
-        if (cutc_blas_ != CUBLAS_STATUS_SUCCESS) {                                    \
-            cutc_set_error(CUTC_ERR_CUDA, "%s:%d %s: cuBLAS status %d", __FILE__,     \
-                           __LINE__, #expr, (int)cutc_blas_);                         \
-            return cutc_blas_ == CUBLAS_STATUS_ALLOC_FAILED ? CUTC_ERR_NO_MEMORY : CUTC_ERR_CUDA; \
-        }                                                                             \
-    } while (0)
 
 // ---------------------------------------------------------------------------
 // engine and workspace
@@ -206,11 +195,6 @@ int make_engine(int dev, Engine **out)
         delete E;
         return CUTC_ERR_CUDA;
     }
-    if (cublasCreate(&E->blas) != CUBLAS_STATUS_SUCCESS) {
-        cutc_set_error(CUTC_ERR_CUDA, "cublasCreate failed");
-        delete E;
-        return CUTC_ERR_CUDA;
-    }
     *out = E;
     return CUTC_OK;
 }
@@ -227,7 +211,6 @@ void destroy_engine(Engine *E)
         cudaEventDestroy(e);
     for (int k = 0; k < kNumEvents; k++)
         cudaEventDestroy(E->ev[k]);
-    cublasDestroy(E->blas);
     cudaStreamSynchronize(E->xfer);
     cudaStreamDestroy(E->xfer);
     cudaStreamDestroy(E->stream);
@@ -358,7 +341,7 @@ static int validate(const Request &R)
 enum Slot {
     S_R1, S_WR1, S_R2, S_WR2, S_RN, S_AOS1, S_AOS2, S_COEF, S_EXPS, S_OFF,
     S_T1, S_F2, S_P, S_G, S_XP, S_S0, S_SL, S_H, S_N, S_XOUT, S_XOUT1, S_IOUT, S_IOUT1,
-    S_R2D, S_F2D, S_POLY, S_BLASWS, S_BASIS,
+    S_R2D, S_F2D, S_POLY, S_BASIS,
     S_SPLIT0  // split-form slots follow
 };
 
@@ -432,11 +415,15 @@ static size_t int2e_row_bytes(const Request &R)
 // r1 rows per X tile and per int_2e block for a budget (each gets the budget): the
 // int_2e contractions run once per block, with K = its rows, so the block is made
 // as large as its budget allows and cut into equal X tiles that each fit theirs.
-// CUTC_TILE_ROWS / CUTC_INT2E_ROWS cap them.
+// CUTC_TILE_ROWS / CUTC_INT2E_ROWS cap them.  A tile has at most kMaxTileRows rows:
+// the pair kernels give each CTA at most 8 r1 rows along gridDim.y (<= 65535).
+constexpr int64_t kMaxTileRows = (int64_t)1 << 18;
+
 static void plan_rows(const Request &R, size_t budget, int64_t *n1t, int64_t *kb)
 {
     const int64_t n1 = R.n1;
     int64_t t = std::max<int64_t>(1, std::min<int64_t>((int64_t)(budget / r1_row_bytes(R)), n1));
+    t = std::min(t, kMaxTileRows);
     if (R.tile_rows > 0)
         t = std::min<int64_t>(t, R.tile_rows);
     if (R.x_only) {  // no int_2e: the block is the tile
@@ -731,13 +718,6 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
                       (size_t)nb * nA2 * 8);
         return CUTC_OK;
     };
-    // cuBLAS gets its workspace from the engine (no allocation inside a build)
-    CUBLAS_TRY(cublasSetStream(E->blas, st));
-    if (R.precision == CUTC_PLAIN_FP64) {
-        const size_t blas_ws = (size_t)32 << 20;
-        CUTC_TRY(W.get(S_BLASWS, blas_ws, &p));
-        CUBLAS_TRY(cublasSetWorkspace(E->blas, p, blas_ws));
-    }
     int64_t blk0 = 0;                                  // first r1 row of the int_2e block
     int blk_rows = (int)std::min<int64_t>(kb, n1);     // its rows (whole tiles)
     bool first_blk = true;
@@ -788,10 +768,9 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
             const double one = 1.0, zero = 0.0;
             if (tev)
                 CUTC_CUDA_TRY(cudaEventRecord(tev[2], st));
-            CUBLAS_TRY(cublasDgemmStridedBatched(
-                E->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)np, nb, n2, &one, d_P, n2, 0, d_G, n2,
-                (long long)nb * n2, &zero, d_Xt + (int64_t)ib * np, (int)np,
-                (long long)blk_rows * np, 4));
+            CUTC_TRY(fp64_gemm(st, true, (int)np, nb, n2, one, d_P, n2, 0, d_G, n2,
+                               (int64_t)nb * n2, zero, d_Xt + (int64_t)ib * np, np,
+                               (int64_t)blk_rows * np, 4));
             if (tev)
                 CUTC_CUDA_TRY(cudaEventRecord(tev[3], st));
         } else {
@@ -819,13 +798,12 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
                 E->tag_i = K == n1 ? R.mol_tag : 0;
                 E->tag_i_buf = d_S0;
                 const double one = 1.0, mhalf = -0.5, beta = first_blk ? 0.0 : 1.0;
-                CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)np, K,
-                                       &one, d_Xt + 3 * (int64_t)K * np, (int)np, d_S0, K, &beta,
-                                       d_H, (int)np));
+                CUTC_TRY(fp64_gemm(st, false, (int)np, (int)np, K, one,
+                                   d_Xt + 3 * (int64_t)K * np, np, 0, d_S0, K, 0, beta, d_H, np,
+                                   0, 1));
                 if (nl > 0)
-                    CUBLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)np, (int)nl,
-                                           3 * K, &mhalf, d_Xt, (int)np, d_Sl, 3 * K, &beta, d_N,
-                                           (int)np));
+                    CUTC_TRY(fp64_gemm(st, false, (int)np, (int)nl, 3 * (int64_t)K, mhalf, d_Xt,
+                                       np, 0, d_Sl, 3 * (int64_t)K, 0, beta, d_N, np, 0, 1));
             } else {
                 CUTC_TRY(split_int2e_tile(E, R, st, sp, w1, a1, n1, K, d_Xt, d_H, d_N, first_blk));
             }
@@ -1221,6 +1199,20 @@ extern "C" int cutc_split_gemm_dev(int n_slices, int M, int N, long long K, cons
     return split_gemm_dense(E, E->stream, n_slices, M, N, K, A, B, C, ldc);
 }
 
+extern "C" int cutc_fp64_gemm_dev(int a_kmajor, int M, int N, long long K, double alpha,
+                                  const double *A, long long lda, long long stride_a,
+                                  const double *B, long long ldb, long long stride_b, double beta,
+                                  double *C, long long ldc, long long stride_c, int batch)
+{
+    Engine *E = nullptr;
+    CUTC_TRY(get_engine(&E));
+    std::lock_guard<std::mutex> lk(E->mu);
+    CUTC_TRY(fp64_gemm(E->stream, a_kmajor != 0, M, N, K, alpha, A, lda, stride_a, B, ldb,
+                       stride_b, beta, C, ldc, stride_c, batch));
+    CUTC_CUDA_TRY(cudaStreamSynchronize(E->stream));
+    return CUTC_OK;
+}
+
 extern "C" int cutc_validate_launch_dims(int gx, int gy, int gz, int bx, int by, int bz)
 {
     Engine *E = nullptr;
@@ -1342,7 +1334,7 @@ extern "C" int cutc_plan(const cutc_options *opt, int n_grid1, int n_grid2, int 
         const int64_t per = split_k_blocks_per_launch(nkb * 32, opt->k_split);
         plan->x_launches_per_tile = (int)((nkb + per - 1) / per);
     } else {
-        plan->x_launches_per_tile = 1;  // one cuBLAS strided-batched DGEMM
+        plan->x_launches_per_tile = 1;  // one FP64 GEMM launch over the four components
     }
     return CUTC_OK;
 }

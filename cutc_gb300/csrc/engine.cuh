@@ -1,7 +1,6 @@
 // Engine context, workspace and request description (host side).
 #pragma once
 
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -43,7 +42,6 @@ struct Engine {
     int max_grid[3] = {0, 0, 0};
     cudaStream_t stream = nullptr;
     cudaStream_t xfer = nullptr;  // device-to-host copies of finished r1 tiles
-    cublasHandle_t blas = nullptr;
     cudaEvent_t ev[kNumEvents];
     std::vector<cudaEvent_t> tile_ev;  // per-tile timing events (grown on demand)
     Workspace ws;
@@ -85,7 +83,7 @@ struct Request {
 };
 
 int get_engine(Engine **out);
-// A private execution context (stream, cuBLAS handle, events, workspace) on device dev.
+// A private execution context (streams, events, workspace) on device dev.
 int make_engine(int dev, Engine **out);
 void destroy_engine(Engine *E);
 // Device bytes one build needs besides its molecule arrays, for a given r1-tile budget.

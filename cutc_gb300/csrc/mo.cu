@@ -11,15 +11,15 @@
 //     T(i, b, g) = sum_a L(a, i) X(a, b, g)        one DGEMM (n_mo x n_ao*nb x n_ao)
 //     Y(i, j, g) = sum_b T(i, b, g) R(b, j)        strided-batched DGEMM over g
 //     X_mo(g, m, i, j) = Y(i, j, g)               tiled transpose (coalesced both ways)
-// FP64 throughout (cuBLAS DGEMM), which is 4 n_mo n_ao (n_ao + n_mo) n1 flops
+// FP64 throughout (the FP64 DMMA GEMM of the plain form), which is 4 n_mo n_ao (n_ao + n_mo) n1 flops
 // per component.
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <mutex>
 
 #include "common.cuh"
+#include "dgemm.cuh"
 #include "engine.cuh"
 
 namespace cutc {
@@ -58,18 +58,7 @@ static int launch_transpose(cudaStream_t st, const double *src, int64_t lds, int
     return CUTC_OK;
 }
 
-#define MO_BLAS_TRY(expr)                                                                   \
-    do {                                                                                    \
-        cublasStatus_t cutc_blas_ = (expr);                                                 \
-        if (cutc_blas_ != CUBLAS_STATUS_SUCCESS) {                                          \
-            cutc_set_error(CUTC_ERR_CUDA, "%s:%d %s: cuBLAS status %d", __FILE__, __LINE__, \
-                           #expr, (int)cutc_blas_);                                         \
-            return cutc_blas_ == CUBLAS_STATUS_ALLOC_FAILED ? CUTC_ERR_NO_MEMORY            \
-                                                            : CUTC_ERR_CUDA;                \
-        }                                                                                   \
-    } while (0)
-
-enum MoSlot { M_L = 180, M_R, M_T, M_Y, M_XIN, M_XOUT, M_WS };
+enum MoSlot { M_L = 180, M_R, M_T, M_Y, M_XIN, M_XOUT };
 
 static int x_ao_to_mo(Engine *E, cudaStream_t st, int n1, int nA, int n_mo, int comps,
                       const double *L, const double *R, const double *x_ao, double *x_mo,
@@ -102,9 +91,6 @@ static int x_ao_to_mo(Engine *E, cudaStream_t st, int n1, int nA, int n_mo, int 
         CUTC_TRY(W.get(M_XOUT, (size_t)n_mo * n_mo * nb * 8, &p));
         Xout = (double *)p;
     }
-    CUTC_TRY(W.get(M_WS, (size_t)32 << 20, &p));
-    MO_BLAS_TRY(cublasSetStream(E->blas, st));
-    MO_BLAS_TRY(cublasSetWorkspace(E->blas, p, (size_t)32 << 20));
     const double one = 1.0, zero = 0.0;
     const int64_t nA2 = (int64_t)nA * nA, nm2 = (int64_t)n_mo * n_mo;
     const int64_t ldo = (int64_t)comps * n1;  // X_mo: g + n1 m + ldo (i + n_mo j)
@@ -117,12 +103,11 @@ static int x_ao_to_mo(Engine *E, cudaStream_t st, int n1, int nA, int n_mo, int 
                 X = Xin;
             }
             // T(i, (b, g)) = L^T X(a, (b, g))
-            MO_BLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_T, CUBLAS_OP_N, n_mo, nA * gb, nA, &one, dL,
-                                    nA, X, nA, &zero, T, n_mo));
+            CUTC_TRY(fp64_gemm(st, true, n_mo, nA * gb, nA, one, dL, nA, 0, X, nA, 0, zero, T,
+                               n_mo, 0, 1));
             // Y_g = T_g R for every g of the block
-            MO_BLAS_TRY(cublasDgemmStridedBatched(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, n_mo, n_mo, nA,
-                                                  &one, T, n_mo, (long long)n_mo * nA, dR, nA, 0,
-                                                  &zero, Y, n_mo, (long long)nm2, gb));
+            CUTC_TRY(fp64_gemm(st, false, n_mo, n_mo, nA, one, T, n_mo, (int64_t)n_mo * nA, dR,
+                               nA, 0, zero, Y, n_mo, nm2, gb));
             // X_mo(g, m, (i, j)) = Y((i, j), g)
             if (dev) {
                 CUTC_TRY(launch_transpose(st, Y, nm2, gb, (int)nm2, x_mo + (int64_t)m * n1 + g0, ldo));

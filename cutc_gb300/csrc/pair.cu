@@ -244,15 +244,15 @@ int launch_pair_f64(cudaStream_t st, const PairArgs &P)
 // ---------------------------------------------------------------------------
 // Allocation-free pair terms
 //
-// Some callers cannot let a library allocate device memory: code that is
-// being captured into a CUDA graph or runs inside a latency-critical serving
-// loop (cudaMalloc / cudaFree synchronise the device and are not allowed
-// during capture), and host programs whose own memory manager owns the whole
-// device.  cutc_jast_bh_dev_noalloc serves them: its scratch (the per-point
-// nucleus terms, the r2 e-n terms and the compact Jastrow term table) lives
-// in the static array below, sized once at load time, so a call allocates
-// nothing -- no cudaMalloc, no cudaFree, no library allocator, no engine
-// context.  The caller still provides the inputs and the output.
+// Some callers cannot let a library allocate device memory: host programs
+// whose own memory manager has reserved the whole device, and latency-critical
+// serving loops in which cudaMalloc / cudaFree would stall on device-wide
+// synchronisation.  cutc_jast_bh_dev_noalloc serves them: its scratch (the
+// per-point nucleus terms, the r2 e-n terms and the compact Jastrow term
+// table) lives in the static array below, sized once at load time, so a call
+// allocates nothing -- no cudaMalloc, no cudaFree, no library allocator, no
+// engine context.  The caller still provides the inputs and the output.  Each
+// call synchronises its stream and reads the status word back.
 // ---------------------------------------------------------------------------
 
 namespace cutc {
@@ -378,7 +378,7 @@ extern "C" int cutc_jast_bh_dev_noalloc(int i0, int n1b, int n_grid1, int n_grid
     PairArgs P;
     P.i0 = i0; P.n1b = n1b; P.n2 = n_grid2; P.nN = n_nuc;
     // the kernel reads the term count from off[nN]; size its shared memory for the maximum
-    P.n_terms = std::min(kMaxTerms, n_nuc * size_bh);
+    P.n_terms = (int)std::min<int64_t>(kMaxTerms, (int64_t)n_nuc * size_bh);
     P.r1 = r1; P.r2 = r2; P.t1 = t1; P.f2 = f2;
     P.coef = coef; P.exps = exps; P.term_off = off; P.a_ee = a_ee;
     P.G = grad1u; P.ldg = n_grid2; P.plane = (int64_t)n1b * n_grid2;

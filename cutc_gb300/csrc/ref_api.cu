@@ -24,8 +24,7 @@
 //     packed AO pairs; plain FP64 unless CUTC_PRECISION=split) without int_2e;
 //   * get_int_2e_ao contracts the caller's full X (it need not be symmetric in
 //     the AO pair) against the short-range products in r1 blocks sized to a
-//     byte budget, with cuBLAS DGEMM accumulating in FP64, then adds A^T.
-#include <cublas_v2.h>
+//     byte budget, with the FP64 DMMA GEMM accumulating in FP64, then adds A^T.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -34,6 +33,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "dgemm.cuh"
 #include "engine.cuh"
 
 namespace cutc {
@@ -117,18 +117,7 @@ static bool ao_count_ok(const char *what, int n_ao)
 }
 
 // Slots of the engine workspace used here (the build's own slots are below 180).
-enum RefSlot { R_S0 = 200, R_S, R_BLASWS };
-
-#define REF_BLAS_TRY(expr)                                                                  \
-    do {                                                                                    \
-        cublasStatus_t cutc_blas_ = (expr);                                                 \
-        if (cutc_blas_ != CUBLAS_STATUS_SUCCESS) {                                          \
-            cutc_set_error(CUTC_ERR_CUDA, "%s:%d %s: cuBLAS status %d", __FILE__, __LINE__, \
-                           #expr, (int)cutc_blas_);                                         \
-            return cutc_blas_ == CUBLAS_STATUS_ALLOC_FAILED ? CUTC_ERR_NO_MEMORY            \
-                                                            : CUTC_ERR_CUDA;                \
-        }                                                                                   \
-    } while (0)
+enum RefSlot { R_S0 = 200, R_S };
 
 // int_2e = A + A^T with A = X_3 S0 - 1/2 sum_m X_m S_m over all n1 r1 points,
 // X (nA^2, n1, 4) the caller's full array; r1 blocks of K rows, FP64 accumulation.
@@ -148,10 +137,6 @@ static int int2e_from_full_x(Engine *E, cudaStream_t st, int n1, int nA, const d
     double *S0 = (double *)p;
     CUTC_TRY(W.get(R_S, 3 * (size_t)K * nA2 * 8, &p));
     double *S = (double *)p;
-    const size_t ws_bytes = (size_t)32 << 20;
-    CUTC_TRY(W.get(R_BLASWS, ws_bytes, &p));
-    REF_BLAS_TRY(cublasSetStream(E->blas, st));
-    REF_BLAS_TRY(cublasSetWorkspace(E->blas, p, ws_bytes));
     const double one = 1.0, mhalf = -0.5;
     for (int g0 = 0; g0 < n1; g0 += K) {
         const int Kb = std::min(K, n1 - g0);
@@ -160,14 +145,14 @@ static int int2e_from_full_x(Engine *E, cudaStream_t st, int n1, int nA, const d
         CUTC_TRY(launch_full_antisym(st, Kb, nA, w1 + g0, aos1 + g0, n1, S, Kb, 3 * (int64_t)Kb));
         const double beta0 = g0 == 0 ? 0.0 : 1.0;
         // I = X_3 S0 (+ I)   (src/build_int_2e_ao.cu:60-67)
-        REF_BLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)nA2, (int)nA2, Kb, &one,
-                                 X + nA2 * (3 * (int64_t)n1 + g0), (int)nA2, S0, Kb, &beta0, I,
-                                 (int)nA2));
+        CUTC_TRY(fp64_gemm(st, false, (int)nA2, (int)nA2, Kb, one,
+                           X + nA2 * (3 * (int64_t)n1 + g0), nA2, 0, S0, Kb, 0, beta0, I, nA2, 0,
+                           1));
         // I += -1/2 X_m S_m   (src/build_int_2e_ao.cu:97-104, one product per component)
         for (int m = 0; m < 3; m++)
-            REF_BLAS_TRY(cublasDgemm(E->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)nA2, (int)nA2, Kb,
-                                     &mhalf, X + nA2 * ((int64_t)m * n1 + g0), (int)nA2,
-                                     S + (int64_t)m * Kb, 3 * Kb, &one, I, (int)nA2));
+            CUTC_TRY(fp64_gemm(st, false, (int)nA2, (int)nA2, Kb, mhalf,
+                               X + nA2 * ((int64_t)m * n1 + g0), nA2, 0, S + (int64_t)m * Kb,
+                               3 * (int64_t)Kb, 0, one, I, nA2, 0, 1));
     }
     return CUTC_OK;
 }

@@ -3,7 +3,7 @@
 // No counterpart in the reference (CuTC serves one synchronous call at a
 // time).  Requests of any molecule, basis and grid size are submitted from
 // any thread and complete asynchronously:
-//   * n_slots workers each own an execution context (stream, cuBLAS handle,
+//   * n_slots workers each own an execution context (stream,
 //     events, workspace); a free worker takes the first queued request whose
 //     device footprint fits the memory budget, so later small requests are
 //     admitted while an earlier large one waits for memory, and requests in

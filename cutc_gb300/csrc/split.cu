@@ -482,40 +482,42 @@ __device__ __forceinline__ void split_digits(double x, int e, __nv_bfloat16 (&ou
 
 // slices[(s * Mpad + r) * Kpad + k] for r < Mpad, k < Kpad (zeros outside M x K);
 // ex[r] = row exponent.  Four consecutive k per thread (Kpad is a multiple of 32),
-// so each slice plane gets one 8-byte store per thread.
+// so each slice plane gets one 8-byte store per thread.  Rows are taken
+// blockIdx.y, blockIdx.y + gridDim.y, ...: any row count fits the grid.
 template <int S, class Src>
 __global__ void slice_kernel(Src src, int M, int64_t K, int64_t Kpad, int Mpad,
                              const unsigned long long *rmax, __nv_bfloat16 *slices, int *ex)
 {
-    const int r = blockIdx.y;
     const int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
     if (k >= Kpad)
         return;
-    const int e = r < M ? row_exponent(rmax[r]) : 0;
-    if (k == 0)
-        ex[r] = e;
-    __nv_bfloat16 d[4][S];
+    for (int r = blockIdx.y; r < Mpad; r += gridDim.y) {
+        const int e = r < M ? row_exponent(rmax[r]) : 0;
+        if (k == 0)
+            ex[r] = e;
+        __nv_bfloat16 d[4][S];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-        if constexpr (Src::kDoubleFloat) {
-            const float2 v = (r < M && k + q < K) ? src.pair(r, k + q) : make_float2(0.f, 0.f);
-            digits_of<S>(digits::scaled_round_df<S>(v.x, v.y, e), d[q]);
-        } else {
-            const double x = (r < M && k + q < K) ? src(r, k + q) : 0.0;
-            split_digits<S>(x, e, d[q]);
+        for (int q = 0; q < 4; q++) {
+            if constexpr (Src::kDoubleFloat) {
+                const float2 v = (r < M && k + q < K) ? src.pair(r, k + q) : make_float2(0.f, 0.f);
+                digits_of<S>(digits::scaled_round_df<S>(v.x, v.y, e), d[q]);
+            } else {
+                const double x = (r < M && k + q < K) ? src(r, k + q) : 0.0;
+                split_digits<S>(x, e, d[q]);
+            }
         }
-    }
 #pragma unroll
-    for (int s = 0; s < S; s++) {
-        __nv_bfloat162 lo, hi;
-        lo.x = d[0][s];
-        lo.y = d[1][s];
-        hi.x = d[2][s];
-        hi.y = d[3][s];
-        uint2 w;
-        w.x = *reinterpret_cast<unsigned *>(&lo);
-        w.y = *reinterpret_cast<unsigned *>(&hi);
-        *reinterpret_cast<uint2 *>(slices + ((int64_t)s * Mpad + r) * Kpad + k) = w;
+        for (int s = 0; s < S; s++) {
+            __nv_bfloat162 lo, hi;
+            lo.x = d[0][s];
+            lo.y = d[1][s];
+            hi.x = d[2][s];
+            hi.y = d[3][s];
+            uint2 w;
+            w.x = *reinterpret_cast<unsigned *>(&lo);
+            w.y = *reinterpret_cast<unsigned *>(&hi);
+            *reinterpret_cast<uint2 *>(slices + ((int64_t)s * Mpad + r) * Kpad + k) = w;
+        }
     }
 }
 
@@ -633,16 +635,12 @@ static int slice_rows(cudaStream_t st, Src src, Operand &op, bool have_rmax = fa
             CUTC_CUDA_TRY(cudaGetLastError());
         }
     }
-    if (op.Mpad > 65535) {
-        cutc_set_error(CUTC_ERR_INVALID, "operand with %d rows exceeds the slicer grid", op.Mpad);
-        return CUTC_ERR_INVALID;
-    }
     if (op.Kpad % 4) {
         cutc_set_error(CUTC_ERR_INVALID, "operand K padding %lld is not a multiple of 4",
                        (long long)op.Kpad);
         return CUTC_ERR_INVALID;
     }
-    dim3 g2(ceil_div(op.Kpad, 4 * 256), (unsigned)op.Mpad);
+    dim3 g2(ceil_div(op.Kpad, 4 * 256), (unsigned)std::min(op.Mpad, 65535));
     slice_kernel<S, Src><<<g2, 256, 0, st>>>(src, op.M, op.K, op.Kpad, op.Mpad, op.rmax,
                                              (__nv_bfloat16 *)op.sl, op.ex);
     CUTC_CUDA_TRY(cudaGetLastError());

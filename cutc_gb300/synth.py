@@ -291,6 +291,23 @@ def scaled_config(name: str, frac1: float = 1.0, frac2: float = 1.0) -> Problem:
     return make_problem(**kw)
 
 
+def r1_sample(p: Problem, ns: int) -> Problem:
+    """The same molecule with ns r1 points spread evenly over its whole r1 grid
+    (every nucleus' shells are represented); r2 and the basis are unchanged."""
+    idx = np.unique(np.linspace(0, p.n_grid1 - 1, ns).round().astype(np.int64))
+    assert len(idx) == ns
+    aos1 = None if p.aos1 is None else np.ascontiguousarray(p.aos1[:, :, idx])
+    return dataclasses.replace(p, r1=np.ascontiguousarray(p.r1[idx]),
+                               wr1=np.ascontiguousarray(p.wr1[idx]), aos1=aos1)
+
+
+def serving_molecule(n_nuc: int = 20, n_ao: int = 250, seed: int = 4242) -> Problem:
+    """A molecule of the serving stream's shape (n_grid1 = 1000 n_nuc,
+    n_grid2 = 4000 n_nuc, 9 Jastrow terms per atom)."""
+    return make_problem(n_nuc=n_nuc, n_ao=n_ao, n_grid1=1000 * n_nuc, n_grid2=4000 * n_nuc,
+                        size_bh=9, seed=seed, box=1.5 + 0.4 * n_nuc)
+
+
 def add_coalescence(p: Problem, k: int = 4) -> Problem:
     """Copy some r1 points and nuclei into r2 (and nuclei into r1) exactly.
 

@@ -29,7 +29,7 @@ extern "C" {
 #define CUTC_ERR_LAUNCH_DIMS (-1) /* same code and condition as src/cutc_int.c:79-86 */
 #define CUTC_ERR_INVALID (-2)     /* bad size, NULL pointer, exponent outside [0, 6] */
 #define CUTC_ERR_NO_MEMORY (-3)   /* device memory exhausted even after tiling */
-#define CUTC_ERR_CUDA (-4)        /* CUDA / cuBLAS failure (message in cutc_last_error) */
+#define CUTC_ERR_CUDA (-4)        /* CUDA failure (message in cutc_last_error) */
 #define CUTC_ERR_NO_DEVICE (-5)   /* no usable sm_103 GPU */
 #define CUTC_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up */
 
@@ -157,23 +157,29 @@ int cutc_jast_bh_dev(int i0, int n1b, int n_grid1, int n_grid2, int n_nuc, int s
 
 /*
  * cutc_jast_bh_dev without any allocation, for callers that cannot let a
- * library allocate device memory: code being captured into a CUDA graph or
- * running in a latency-critical serving loop (cudaMalloc and cudaFree
- * synchronise the device and are not allowed during capture), and programs
- * whose own memory manager owns the whole device.  No counterpart in the
- * reference.
+ * library allocate device memory: programs whose own memory manager has
+ * reserved the whole device (a framework's caching allocator holding all of
+ * HBM, where a cudaMalloc from a library fails or fragments that pool), and
+ * latency-critical serving loops, where cudaMalloc and cudaFree would stall
+ * on device-wide synchronisation.  No counterpart in the reference.
  *
  * Same arguments, layout and results as cutc_jast_bh_dev, plus the stream to
- * run on (NULL = the legacy default stream); synchronous on that stream.  Its
+ * run on (NULL = the legacy default stream).  Each call waits for its stream
+ * to finish and reads a status word back to the host before it returns.  Its
  * scratch -- per-point nucleus terms, r2 e-n terms and the Jastrow term table,
  * 32 * n1b * n_nuc + 8 * n_grid2 * n_nuc bytes plus ~130 KB -- lives in a
  * fixed 32 MiB device array that every GPU loading this library holds until
- * exit; larger requests are rejected with CUTC_ERR_INVALID and a message.  It
- * calls no cudaMalloc, cudaFree or allocating library routine and creates no
- * engine context.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress, with that device current): make that first
- * call before any stream capture.  All calls share the one array, so calls
- * that overlap on the GPU (different streams or threads) race: serialise them.
+ * exit; larger requests are rejected with CUTC_ERR_INVALID and a message
+ * before anything runs.  It calls no cudaMalloc, cudaFree or allocating
+ * library routine and creates no engine context.  The first call on a device
+ * also does the set-up: it looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current), so make that first call
+ * before any stream capture.  All calls share the one array and each call
+ * overwrites what the previous one left there, so calls that overlap on the
+ * GPU (different streams or threads) race: serialise them.  Exponents outside
+ * [0, 6] and more than 4096 kept terms are found on the device, while the pair
+ * kernel runs: the call then returns CUTC_ERR_INVALID with grad1u already
+ * overwritten.
  */
 int cutc_jast_bh_dev_noalloc(int i0, int n1b, int n_grid1, int n_grid2, int n_nuc, int size_bh,
                              const double *r1, const double *r2, const double *rn,
@@ -193,6 +199,23 @@ int cutc_split_gemm_dev(int n_slices, int M, int N, long long K,
                         const double *A, const double *B, double *C, long long ldc);
 
 /*
+ * The plain form's FP64 contraction alone, on device arrays of the current
+ * device, with cuBLAS's column-major argument meaning (the reference's
+ * cublasDgemm calls, src/build_int2_grad1_u12_ao.cu:152-159 and
+ * src/build_int_2e_ao.cu:60-67,97-104, take these operand orders):
+ *   C[m + ldc n] = alpha sum_k opA(m, k) B[n ldb + k] + beta C[m + ldc n]
+ * for m < M, n < N and each of `batch` problems, whose A, B and C start
+ * stride_a, stride_b and stride_c doubles apart.  opA(m, k) = A[m lda + k]
+ * when a_kmajor is non-zero (cuBLAS OP_T), else A[k lda + m] (OP_N); B is
+ * OP_N.  C is not read when beta == 0.  FP64 DMMA tensor-core tiles; no
+ * allocation.  Synchronous on the engine stream.
+ */
+int cutc_fp64_gemm_dev(int a_kmajor, int M, int N, long long K, double alpha, const double *A,
+                       long long lda, long long stride_a, const double *B, long long ldb,
+                       long long stride_b, double beta, double *C, long long ldc,
+                       long long stride_c, int batch);
+
+/*
  * The launch-geometry check of src/cutc_int.c:79-86 against the current
  * device: block volume > maxThreadsPerBlock or any grid extent > maxGridSize
  * (unsigned comparisons, as the reference's dim3 arithmetic) returns
@@ -202,8 +225,8 @@ int cutc_validate_launch_dims(int nxBlocks, int nyBlocks, int nzBlocks,
                               int blockxSize, int blockySize, int blockzSize);
 
 /* ---- serving: continuous batching on one GPU (no reference counterpart) --
- * A server owns n_slots execution contexts (stream, cuBLAS handle,
- * workspace) and a worker thread each.  Submitted requests are queued; a free
+ * A server owns n_slots execution contexts (stream, events, workspace) and a
+ * worker thread each.  Submitted requests are queued; a free
  * worker takes the first queued request whose device footprint fits the
  * memory budget next to the requests in flight (a request that does not fit
  * runs alone), so requests overlap on the GPU as slots and memory free up.

@@ -115,6 +115,59 @@ def x_block(p, P: np.ndarray, i0: int, n1b: int) -> np.ndarray:
     return X
 
 
+def x_rows(p, i0: int = 0, n1b: int | None = None, window_bytes: int = 1 << 30) -> np.ndarray:
+    """X for r1 rows [i0, i0+n1b), all 4 components, without the whole P.
+
+    P is formed by the C restatement one r2 window at a time
+    (src/long_range_integ.cu:21-45 on a window, as the reference's r2 passes do,
+    src/build_int2_grad1_u12_ao.cu:113-331) and each window's share
+    G_m[:, window] P_window^T is added: the same products as x_block, summed in
+    r2 windows.  For molecules whose full P (nA^2 x n2 doubles) does not fit."""
+    n1b = p.n_grid1 - i0 if n1b is None else n1b
+    G = pair(p, i0, n1b).reshape(4 * n1b, p.n_grid2)
+    nA2 = p.n_ao * p.n_ao
+    n2 = p.n_grid2
+    jc = int(max(1, min(n2, window_bytes // (8 * nA2))))
+    X = np.zeros((4 * n1b, nA2))
+    Pw = np.empty((nA2, jc))
+    for j0 in range(0, n2, jc):
+        w = min(jc, n2 - j0)
+        Pv = Pw[:, :w] if w == jc else np.empty((nA2, w))
+        lib().oracle_long_range(j0, w, n2, p.n_ao, _dp(p.wr2), _dp(p.aos2), _dp(Pv))
+        X += np.ascontiguousarray(G[:, j0:j0 + w]) @ Pv.T
+    return X.reshape(4, n1b, nA2)
+
+
+def int2e_rows(p, X4: np.ndarray, rows, S0=None, S=None) -> np.ndarray:
+    """Rows `rows` of int_2e (C layout, i.e. Fortran columns) for the r1 points
+    of p, from their X (4, n1, nA^2): (A + A^T)[rows, :] with A as int2e_from_x
+    returns it, without forming the nA^2 x nA^2 matrix."""
+    rows = np.asarray(rows)
+    if S0 is None:
+        S0 = short_herm(p)
+    if S is None:
+        S = short_nonherm(p)
+    out = S0[rows] @ X4[3] + (S0 @ X4[3][:, rows]).T
+    for m in range(3):
+        out -= 0.5 * (S[rows, m] @ X4[m] + (S[:, m] @ X4[m][:, rows]).T)
+    return out
+
+
+def int2e_matvec(p, X4: np.ndarray, v: np.ndarray, S0=None, S=None) -> np.ndarray:
+    """int_2e (C layout) times v, for the r1 points of p, from their X:
+    (A + A^T) v = S0 (X_3 v) + X_3^T (S0^T v) - 1/2 sum_m [...], without
+    forming the nA^2 x nA^2 matrix."""
+    if S0 is None:
+        S0 = short_herm(p)
+    if S is None:
+        S = short_nonherm(p)
+    out = S0 @ (X4[3] @ v) + X4[3].T @ (S0.T @ v)
+    for m in range(3):
+        Sm = S[:, m]
+        out -= 0.5 * (Sm @ (X4[m] @ v) + X4[m].T @ (Sm.T @ v))
+    return out
+
+
 def int2e_from_x(p, X4: np.ndarray, i0: int = 0, S0=None, S=None) -> np.ndarray:
     """Contraction of X (4, n1b, nA^2) over its r1 rows, before A + A^T.
 

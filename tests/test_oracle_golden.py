@@ -70,3 +70,20 @@ def test_oracle_pair_term_symmetries():
     Gs = oracle.pair(scaled)
     np.testing.assert_allclose(Gs[:3], k * G[:3], rtol=0, atol=1e-14 * np.abs(G[:3]).max())
     np.testing.assert_allclose(Gs[3], k * k * G[3], rtol=0, atol=1e-14 * np.abs(G[3]).max())
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_windowed_oracle_matches_reference(name):
+    """x_rows (P formed per r2 window, as for molecules whose whole P does not fit),
+    int2e_rows and int2e_matvec against the reference's own outputs."""
+    p, ref = load_case(name)
+    nA2 = p.n_ao ** 2
+    X4 = oracle.x_rows(p, window_bytes=8 * nA2 * 5)  # r2 windows of 5 points
+    ex = oracle.rel_err(X4[:3], ref["X"])
+    assert ex["norm"] < 1e-13 and ex["max"] < 1e-13, ex
+    rows = np.arange(0, nA2, 3)
+    ei = oracle.rel_err(oracle.int2e_rows(p, X4, rows), ref["int2e"][rows])
+    assert ei["max"] < 1e-13, ei
+    v = np.random.default_rng(5).standard_normal(nA2)
+    ev = oracle.rel_err(oracle.int2e_matvec(p, X4, v), ref["int2e"] @ v)
+    assert ev["max"] < 1e-13, ev

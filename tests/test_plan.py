@@ -49,6 +49,22 @@ def test_plan_medium_is_one_block():
     assert p["block_rows"] == 25000 and p["n_blocks"] == 1 and p["n_tiles"] >= 2
 
 
+def test_plan_tile_rows_fit_the_pair_kernel_grid():
+    # the pair kernels put 8 r1 rows per CTA on gridDim.y (<= 65535): a tile never
+    # exceeds 2^18 rows, however small n_grid2 makes a row
+    for prec in (cg.PLAIN_FP64, cg.SPLIT_BF16):
+        p = cg.plan(2_000_000, 4, 2, 1, prec, device_pointers=True, max_work_bytes=64 << 30)
+        assert p["tile_rows"] <= 1 << 18
+        assert p["n_tiles"] * p["tile_rows"] >= 2_000_000
+
+
+def test_plan_split_tile_past_the_old_slicer_limit():
+    # 20 000 r1 rows x 2 000 r2 points fit one split-form tile: its G operand has
+    # 4 x 20 000 = 80 000 rows, which the slicer handles with grid-stride rows
+    p = cg.plan(20000, 2000, 6, 3, cg.SPLIT_BF16, device_pointers=True, max_work_bytes=24 << 30)
+    assert p["tile_rows"] == 20000 and p["n_tiles"] == 1
+
+
 def test_plan_env_caps(monkeypatch):
     monkeypatch.setenv("CUTC_TILE_ROWS", "40")
     monkeypatch.setenv("CUTC_INT2E_ROWS", "120")
