@@ -50,3 +50,16 @@ def test_highest_exponents(prec):
     p.o_bh = np.ascontiguousarray(np.array([[5, 1, 6, 3], [1, 6, 0, 6]], dtype=np.int32))
     X, I = cg.build_integrals(p, prec)
     _check(X, I, *oracle.cutc_int(p), prec)
+
+
+def test_split_tile_with_more_than_65535_g_rows():
+    """One split-form r1 tile of 20 000 rows: its G operand has 4 x 20 000 = 80 000
+    rows, past the 65 535 blocks a grid dimension holds (the slicer takes rows
+    grid-stride).  The reference tiles any n_grid1 (src/build_int2_grad1_u12_ao.cu:63-99)."""
+    p = synth.make_problem(n_nuc=3, n_ao=6, n_grid1=20000, n_grid2=2000, size_bh=6, seed=41)
+    plan = cg.plan(p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, cg.SPLIT_BF16, max_work_bytes=24 << 30)
+    assert plan["n_tiles"] == 1 and 4 * plan["tile_rows"] > 65535
+    X, I, st = cg.build_integrals(p, cg.SPLIT_BF16, max_work_bytes=24 << 30, with_stats=True)
+    assert st["n_r1_tiles"] == 1
+    Xo, Io = oracle.cutc_int(p)
+    _check(X, I, Xo, Io, cg.SPLIT_BF16)
