@@ -531,6 +531,53 @@ def run_ours(args):
     return 0
 
 
+def run_shard(args):
+    """--shard under torchrun: ONE build per step spread over the ranks by r1 (each
+    rank builds its r1 window's X rows and int_2e share on its GPU, device-resident;
+    one NCCL all-reduce sums the int_2e shares): strong scaling of a single build."""
+    import torch
+    import torch.distributed as dist
+    import cutc_gb300 as cg
+    from cutc_gb300.shard import build_sharded
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist.init_process_group("nccl" if world > 1 else "gloo")
+    prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
+    p = synth.make_config(args.config)
+
+    def step():
+        return build_sharded(p, dist, prec, args.slices if prec else None)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        (b, e), X, I = step()
+    torch.cuda.synchronize(dev)
+    dist.barrier()
+    secs = max_over_ranks(time.perf_counter() - t0, dist if world > 1 else None, dev)
+    if rank == 0:
+        v = args.steps / secs
+        print(json.dumps({
+            "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+            "dtype": "bf16" if prec == cg.SPLIT_BF16 else "f64", "data": "synthetic",
+            "config": {"workload": workload_desc(args.config, p), "precision": args.precision,
+                       "parallelism": "r1 sharded over %d GPUs, one all-reduce of int_2e" % world,
+                       "window_rank0": [b, e]},
+            "e2e": {"value": None, "reason": "each step copies the molecule's host arrays to "
+                                             "every rank's GPU and builds its window there; X "
+                                             "stays on the device"}}), flush=True)
+    dist.destroy_process_group()
+    return 0
+
+
 def rel(a, b):
     from oracle.oracle import rel_err
     return rel_err(a, b)
@@ -1174,6 +1221,8 @@ def main(argv=None):
     ap.add_argument("--skip-serving", action="store_true")
     ap.add_argument("--main-only", action="store_true",
                     help="the medium line alone: skip the CPU, accuracy and extra legs")
+    ap.add_argument("--shard", action="store_true",
+                    help="under torchrun: one build per step, r1 sharded over the ranks")
     ap.add_argument("--serving", action="store_true", help="run the serving stream instead")
     ap.add_argument("--requests", type=int, default=256)
     ap.add_argument("--rate", type=float, default=1.0, help="serving arrivals per second")
@@ -1205,6 +1254,8 @@ def main(argv=None):
         args.skip_large = args.skip_scan = args.skip_serving = True
     if args.kernel:
         return run_kernel(args)
+    if args.shard:
+        return run_shard(args)
     if args.serving:
         return run_serving_cli(args)
     if args.scan:

@@ -83,7 +83,8 @@ class Options(ctypes.Structure):
                 ("x_components", ctypes.c_int), ("device_pointers", ctypes.c_int),
                 ("max_work_bytes", ctypes.c_size_t), ("stream", ctypes.c_void_p),
                 ("pair_fp64", ctypes.c_int), ("k_split", ctypes.c_int),
-                ("int2e_layout", ctypes.c_int), ("basis", ctypes.c_void_p)]
+                ("int2e_layout", ctypes.c_int), ("basis", ctypes.c_void_p),
+                ("r1_begin", ctypes.c_int), ("r1_end", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -238,7 +239,7 @@ def cutc_int(nxBlocks, nyBlocks, nzBlocks, blockxSize, blockySize, blockzSize,
 
 def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_components=3,
             device_pointers=False, max_work_bytes=0, stream=None, pair_fp64=False,
-            k_split=0, int2e_layout=INT2E_PQST, basis=None) -> Options:
+            k_split=0, int2e_layout=INT2E_PQST, basis=None, r1_window=None) -> Options:
     o = Options()
     load().cutc_default_options(ctypes.byref(o))
     o.precision = precision
@@ -255,6 +256,8 @@ def options(precision=PLAIN_FP64, n_slices=None, a_en=1.0, a_ee=1.0, x_component
     if basis is not None:
         o.basis = ctypes.addressof(basis)
         o._basis = basis  # keeps the basis alive with the options
+    if r1_window is not None:
+        o.r1_begin, o.r1_end = int(r1_window[0]), int(r1_window[1])
     return o
 
 

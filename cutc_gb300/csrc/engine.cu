@@ -527,8 +527,16 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         CUTC_TRY(put(S_R2, R.r2, 3 * (size_t)n2 * 8, &d_r2));
         CUTC_TRY(put(S_WR2, R.wr2, (size_t)n2 * 8, &d_wr2));
         CUTC_TRY(put(S_RN, R.rn, 3 * (size_t)nN * 8, &d_rn));
-        if (R.aos1)
+        if (R.aos1 && R.ld1 > n1) {
+            // an r1 window of a larger grid: its 4 nA columns of n1 points, packed
+            CUTC_TRY(W.get(S_AOS1, 4 * (size_t)n1 * nA * 8, &p));
+            CUTC_CUDA_TRY(cudaMemcpy2DAsync(p, (size_t)n1 * 8, R.aos1, (size_t)R.ld1 * 8,
+                                            (size_t)n1 * 8, 4 * (size_t)nA,
+                                            cudaMemcpyHostToDevice, st));
+            d_aos1 = (const double *)p;
+        } else if (R.aos1) {
             CUTC_TRY(put(S_AOS1, R.aos1, 4 * (size_t)n1 * nA * 8, &d_aos1));
+        }
         // only the value component of aos_data2 is used (src/long_range_integ.cu:30-35)
         if (R.aos2)
             CUTC_TRY(put(S_AOS2, R.aos2, (size_t)n2 * nA * 8, &d_aos2v));
@@ -548,6 +556,9 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
             d_aos2v = (const double *)p;
         }
     }
+    // leading dimension of the AO values on r1 on the device: a window of a caller's
+    // device array keeps the caller's stride; uploaded or evaluated arrays are packed
+    const int64_t ld_a1 = (in_dev && R.aos1 && R.ld1 > 0) ? R.ld1 : n1;
     const int nt = (int)exps.size();
     double *d_coef;
     int *d_exps, *d_off;
@@ -791,8 +802,9 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
                 const bool keep =
                     K == n1 && R.mol_tag && E->tag_i == R.mol_tag && E->tag_i_buf == d_S0;
                 if (!keep) {
-                    CUTC_TRY(launch_sym_products(st, K, nA, w1, a1, n1, d_S0, K));
-                    CUTC_TRY(launch_antisym_products(st, K, nA, w1, a1, n1, d_Sl, 3 * (int64_t)K));
+                    CUTC_TRY(launch_sym_products(st, K, nA, w1, a1, ld_a1, d_S0, K));
+                    CUTC_TRY(launch_antisym_products(st, K, nA, w1, a1, ld_a1, d_Sl,
+                                                     3 * (int64_t)K));
                     note_launches(2);
                 }
                 E->tag_i = K == n1 ? R.mol_tag : 0;
@@ -805,7 +817,8 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
                     CUTC_TRY(fp64_gemm(st, false, (int)np, (int)nl, 3 * (int64_t)K, mhalf, d_Xt,
                                        np, 0, d_Sl, 3 * (int64_t)K, 0, beta, d_N, np, 0, 1));
             } else {
-                CUTC_TRY(split_int2e_tile(E, R, st, sp, w1, a1, n1, K, d_Xt, d_H, d_N, first_blk));
+                CUTC_TRY(split_int2e_tile(E, R, st, sp, w1, a1, ld_a1, K, d_Xt, d_H, d_N,
+                                          first_blk));
             }
             first_blk = false;
         }
@@ -1037,6 +1050,24 @@ extern "C" int cutc_int_ex(const cutc_options *opt, int n_grid1, int n_grid2, in
     R.c_bh = c_bh; R.m_bh = m_bh; R.n_bh = n_bh; R.o_bh = o_bh;
     R.X = int2_grad1_u12_ao; R.I = int_2e_ao;
     R.x_only = int_2e_ao == nullptr;
+    if (opt->r1_begin != 0 || opt->r1_end != 0) {
+        // an r1 shard: the window's points of the full arrays
+        if (opt->r1_begin < 0 || opt->r1_end <= opt->r1_begin || opt->r1_end > n_grid1) {
+            cutc_set_error(CUTC_ERR_INVALID, "r1 window [%d, %d) outside [0, n_grid1=%d)",
+                           opt->r1_begin, opt->r1_end, n_grid1);
+            return CUTC_ERR_INVALID;
+        }
+        const int b = opt->r1_begin;
+        R.n1 = opt->r1_end - b;
+        if (R.r1)
+            R.r1 += 3 * (int64_t)b;
+        if (R.wr1)
+            R.wr1 += b;
+        if (R.aos1) {
+            R.aos1 += b;
+            R.ld1 = n_grid1;
+        }
+    }
     const char *tr = getenv("CUTC_TILE_ROWS");
     R.tile_rows = tr ? atoi(tr) : 0;
     const char *ir = getenv("CUTC_INT2E_ROWS");
@@ -1064,8 +1095,8 @@ extern "C" int cutc_int_scan(const cutc_options *opt, int n_sets, int n_grid1, i
         opt = &defaults;
     }
     if (n_sets < 1 || n_grid1 <= 0 || n_grid2 <= 0 || n_ao <= 0 || n_nuc <= 0 || size_bh < 0 ||
-        !int2_grad1_u12_ao || !int_2e_ao) {
-        cutc_set_error(CUTC_ERR_INVALID, "invalid scan arguments");
+        !int2_grad1_u12_ao || !int_2e_ao || opt->r1_begin != 0 || opt->r1_end != 0) {
+        cutc_set_error(CUTC_ERR_INVALID, "invalid scan arguments (an r1 window is not taken)");
         return CUTC_ERR_INVALID;
     }
     static std::atomic<unsigned long long> next_tag{1};

@@ -75,6 +75,8 @@ struct Request {
     int x_only = 0;        // X alone (int_2e output NULL): wr1, aos1 and I are not used
     cudaStream_t stream = nullptr;
     int n1 = 0, n2 = 0, nA = 0, nN = 0, nB = 0;
+    int64_t ld1 = 0;  // leading dimension (points) of aos1 when it is a window of a larger grid
+                      // (0: n1)
     const double *r1 = nullptr, *wr1 = nullptr, *r2 = nullptr, *wr2 = nullptr, *rn = nullptr;
     const double *aos1 = nullptr, *aos2 = nullptr;
     const double *c_bh = nullptr;

@@ -422,6 +422,10 @@ extern "C" int cutc_server_submit(cutc_server *h, const cutc_request *req, unsig
     }
     if ((!req->aos_data1 || !req->aos_data2))
         CUTC_TRY(validate_basis(req->options.basis, req->n_ao));
+    if (req->options.r1_begin != 0 || req->options.r1_end != 0) {
+        cutc_set_error(CUTC_ERR_INVALID, "the server builds whole r1 grids (no r1 window)");
+        return CUTC_ERR_INVALID;
+    }
     auto job = std::make_unique<Job>();
     job->req = *req;
     Request R = to_request(*req);

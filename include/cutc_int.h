@@ -88,6 +88,15 @@ typedef struct cutc_options {
                                leaves it (the order cutc_no uses), written directly */
     const cutc_basis *basis;    /* with aos_data1 and/or aos_data2 NULL: those AO arrays are
                                    evaluated on the device from this basis (NULL: not used) */
+    int r1_begin, r1_end;   /* cutc_int_ex only: an r1 shard.  With r1_end > r1_begin the build
+                               covers r1 points [r1_begin, r1_end) of the full arrays r1, wr1 and
+                               aos_data1 (still laid out for all n_grid1 points); X is written for
+                               those points only, as X(n_ao, n_ao, r1_end - r1_begin, comps),
+                               and int_2e receives that shard's share A_s + A_s^T.  int_2e is
+                               linear in the r1 points, so the shares of shards that partition
+                               [0, n_grid1) sum to the whole build's int_2e (the r1 sharding of
+                               a build over several GPUs; the caller sums the shares, e.g. with
+                               one all-reduce).  0, 0 = the whole grid */
 } cutc_options;
 
 #define CUTC_INT2E_PQST 0
@@ -252,7 +261,8 @@ typedef struct cutc_request {
     const double *r1, *wr1, *r2, *wr2, *rn, *aos_data1, *aos_data2, *c_bh;
     const int *m_bh, *n_bh, *o_bh;
     double *int2_grad1_u12_ao, *int_2e_ao;
-    cutc_options options;       /* device_pointers, stream and max_work_bytes are ignored */
+    cutc_options options;       /* device_pointers, stream and max_work_bytes are ignored; an
+                                   r1 window is refused */
 } cutc_request;
 
 typedef struct cutc_server_stats {
