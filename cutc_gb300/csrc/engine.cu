@@ -379,7 +379,8 @@ static size_t fixed_bytes(const Request &R)
     if (R.precision == CUTC_PLAIN_FP64)
         b += (double)np * n2 * 8;
     else
-        b += (double)split_fixed_bytes(R) + (3.0 + nN) * n2 * sizeof(float2);
+        b += (double)split_fixed_bytes(R) + (3.0 + nN) * n2 * sizeof(float2) +
+             (double)split_pair_fixed_bytes(R);
     if (!(R.device_pointers || R.out_device) && !R.x_only)
         b += 2.0 * int2e_slab_cols(R.nA) * nA * nA * 8;
     return (size_t)b;
@@ -393,7 +394,7 @@ static size_t r1_row_bytes(const Request &R)
     if (!(R.device_pointers || R.out_device))
         b += 2 * (size_t)R.x_components * R.nA * R.nA * 8;
     if (R.precision == CUTC_SPLIT_BF16)
-        b += split_r1_row_bytes(R) + pair_df_poly_bytes(6, 1, R.nN);
+        b += split_r1_row_bytes(R) + pair_df_poly_bytes(6, 1, R.nN) + split_pair_row_bytes(R);
     return b;
 }
 
@@ -668,6 +669,8 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         }
     } else {
         CUTC_TRY(split_prepare_x(E, R, st, d_wr2, d_aos2v, n1t, S_SPLIT0, sp));
+        if (split_pair_tc_ok(R, exps.data(), nt))
+            CUTC_TRY(split_pair_prepare(E, R, st, d_f2, n1t, sp));
     }
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[2], st));
 
@@ -767,8 +770,12 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
             // the kernel also leaves the row maxima the G slicer needs
             CUTC_CUDA_TRY(cudaMemsetAsync(sp.BX.rmax, 0, 4 * (size_t)nb * 8, st));
             P.rmax = sp.BX.rmax;
-            CUTC_TRY(launch_pair_df(st, P, pexp, psparse, d_rn, R.a_en));
-            note_launches(3);
+            if (sp.pair_tc) {
+                CUTC_TRY(split_pair_tile(E, R, st, sp, P, d_rn, R.a_en));
+            } else {
+                CUTC_TRY(launch_pair_df(st, P, pexp, psparse, d_rn, R.a_en));
+                note_launches(3);
+            }
         }
         if (tev)
             CUTC_CUDA_TRY(cudaEventRecord(tev[1], st));

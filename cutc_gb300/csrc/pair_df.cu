@@ -23,11 +23,11 @@
 #include "common.cuh"
 #include "dfloat.cuh"
 #include "pair.cuh"
+#include "pair_near.cuh"
 
 namespace cutc {
 
 constexpr int kDfThreads = 128;
-constexpr float kNearR2 = 1.0e-4f;  // r12^2 below which a pair is done in FP64
 
 template <int E>
 struct PolyLayout {
@@ -117,59 +117,6 @@ __global__ void r2_df_kernel(int n2, int nN, const double *__restrict__ r2,
     }
 }
 
-// One pair in FP64, term by term as the reference kernel does it
-// (src/jast_bh.cu:138-254), for pairs near e-e coalescence.
-__device__ __noinline__ void pair_fp64_single(const PairDfArgs &P, int i, int j, double out[4])
-{
-    const int64_t gi = P.i0 + i;
-    const double dx = P.r1[3 * gi] - P.r2[3 * (int64_t)j];
-    const double dy = P.r1[3 * gi + 1] - P.r2[3 * (int64_t)j + 1];
-    const double dz = P.r1[3 * gi + 2] - P.r2[3 * (int64_t)j + 2];
-    const double d2 = dx * dx + dy * dy + dz * dz;
-    const double a = P.a_ee;
-    double g = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
-    if (d2 > 1e-15) {
-        const double d = sqrt(d2);
-        const double t = 1.0 / (1.0 + a * d);
-        g = a * d * t;
-        const double s = a * t * t / d;
-        gx = s * dx;
-        gy = s * dy;
-        gz = s * dz;
-    }
-    double ux = 0.0, uy = 0.0, uz = 0.0;
-    for (int A = 0; A < P.nN; A++) {
-        const NucTerm t1 = P.t1[(int64_t)i * P.nN + A];
-        const double f1 = t1.f, f2 = P.f2[(int64_t)A * P.n2 + j];
-        for (int k = P.term_off[A]; k < P.term_off[A + 1]; k++) {
-            const int e = P.exps[k];
-            const int m = e & 7, n = (e >> 3) & 7, o = (e >> 6) & 7;
-            double F1[kMaxExp + 1], F2[kMaxExp + 1], Gp[kMaxExp + 1];
-            F1[0] = F2[0] = Gp[0] = 1.0;
-            for (int q = 1; q <= kMaxExp; q++) {
-                F1[q] = F1[q - 1] * f1;
-                F2[q] = F2[q - 1] * f2;
-                Gp[q] = Gp[q - 1] * g;
-            }
-            double t1v = 0.0, t2v = 0.0;
-            if (m > 0)
-                t1v += P.coef[3 * k] * F1[m - 1] * F2[n];
-            if (n > 0)
-                t1v += P.coef[3 * k + 1] * F1[n - 1] * F2[m];
-            t1v *= Gp[o];
-            if (o > 0)
-                t2v = P.coef[3 * k + 2] * Gp[o - 1] * (F1[m] * F2[n] + F1[n] * F2[m]);
-            ux += t1v * t1.gx + t2v * gx;
-            uy += t1v * t1.gy + t2v * gy;
-            uz += t1v * t1.gz + t2v * gz;
-        }
-    }
-    out[0] = ux;
-    out[1] = uy;
-    out[2] = uz;
-    out[3] = -0.5 * (ux * ux + uy * uy + uz * uz);
-}
-
 // Sp: every Jastrow exponent is 0, 2, 3 or 4 (E == 4).  Then U[b][o] and W[b][o'] vanish
 // for b = 1, o = 1 and o' = 0, and the polynomials are evaluated as
 //   sum_{b in 0,2,3,4} f2^b p_b(g) = p_0 + f2^2 (p_2 + f2 (p_3 + f2 p_4)),
@@ -211,7 +158,7 @@ pair_df_kernel(PairDfArgs P)
         const df::D d2 = df::add(df::add(df::sqr(dx), df::sqr(dy)), df::sqr(dz));
         const int64_t o = (int64_t)(row0 + r) * P.ldg + j;
         float2 w4[4];
-        if (d2.hi < kNearR2) {
+        if (d2.hi < kNearPairR2) {
             double v[4];
             pair_fp64_single(P, row0 + r, j, v);
             for (int c = 0; c < 4; c++) {
@@ -322,6 +269,129 @@ pair_df_kernel(PairDfArgs P)
             }
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 operands of the tensor-core pair terms (exponents in {0, 2, 3, 4})
+//
+// For fixed (r1, r2) the nucleus sum of the sparse-power form is linear in the
+// powers f2_A(r2)^b, b in {0, 2, 3, 4}: with k = 4 A + q (b = kPowB[q])
+//   V_c(r1, r2) = sum_k C[(r1, c)][k] F[r2][k],   F[r2][k] = f2_A(r2)^b,
+//   C[(r1, c)][k] = U_A[b][o](r1) (d f1_A / dx)(r1)   c = 0..3,  o = kPowB[c]
+//                   ... d/dy for c = 4..7, d/dz for c = 8..11
+//                   W_A[b][o'](r1), o' = c - 11           c = 12..14
+//                   0                                     c = 15
+// and then, per pair (g = g12 and its gradient, as in pair_df_kernel),
+//   grad1 u = sum_o g^o V_{.,o} + g (V_12 + g (V_13 + g V_14)) grad g.
+// The contraction over k runs on the tensor cores (split.cu, pair_tc_kernel).
+// ---------------------------------------------------------------------------
+__constant__ int kPowB[4] = {0, 2, 3, 4};
+
+// F[j * 4 nN + 4 A + q] = f2[A n2 + j]^b_q, FP64
+__global__ void pair_tc_f_kernel(int n2, int nN, const double *__restrict__ f2,
+                                 double *__restrict__ F)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n2 * nN)
+        return;
+    const int j = (int)(idx / nN), A = (int)(idx % nN);
+    const double f = f2[(int64_t)A * n2 + j];
+    const double f2v = f * f;
+    double *o = F + (int64_t)j * 4 * nN + 4 * A;
+    o[0] = 1.0;
+    o[1] = f2v;
+    o[2] = f2v * f;
+    o[3] = f2v * f2v;
+}
+
+// C[((i 16 + c) 4 nN) + 4 A + q] for rows i of the tile, FP64; the polynomial
+// coefficients U, W are formed as in r1_poly_kernel<4>.
+__global__ void pair_tc_coef_kernel(int i0, int n, int nN, const double *__restrict__ r1,
+                                    const double *__restrict__ rn, double a_en,
+                                    const double *__restrict__ tcoef,
+                                    const int *__restrict__ texps, const int *__restrict__ toff,
+                                    double *__restrict__ C)
+{
+    constexpr int E = 4;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * nN)
+        return;
+    const int i = (int)(idx / nN), A = (int)(idx % nN);
+    const double *p = r1 + 3 * (int64_t)(i0 + i);
+    const double dx = p[0] - rn[3 * A], dy = p[1] - rn[3 * A + 1], dz = p[2] - rn[3 * A + 2];
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    double f = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+    if (d2 > 1e-15) {
+        const double d = sqrt(d2);
+        const double t = 1.0 / (1.0 + a_en * d);
+        f = a_en * d * t;
+        const double sg = a_en * t * t / d;
+        gx = sg * dx;
+        gy = sg * dy;
+        gz = sg * dz;
+    }
+    double F[E + 1];
+    F[0] = 1.0;
+    for (int k = 1; k <= E; k++)
+        F[k] = F[k - 1] * f;
+    double U[(E + 1) * (E + 1)], W[(E + 1) * E];
+    for (int k = 0; k < (E + 1) * (E + 1); k++)
+        U[k] = 0.0;
+    for (int k = 0; k < (E + 1) * E; k++)
+        W[k] = 0.0;
+    for (int k = toff[A]; k < toff[A + 1]; k++) {
+        const int e = texps[k];
+        const int m = e & 7, nn = (e >> 3) & 7, o = (e >> 6) & 7;
+        const double cm = tcoef[3 * k], cn = tcoef[3 * k + 1], co = tcoef[3 * k + 2];
+        if (m > 0)
+            U[nn * (E + 1) + o] += cm * F[m - 1];
+        if (nn > 0)
+            U[m * (E + 1) + o] += cn * F[nn - 1];
+        if (o > 0) {
+            W[nn * E + o - 1] += co * F[m];
+            W[m * E + o - 1] += co * F[nn];
+        }
+    }
+    const int64_t K = 4 * (int64_t)nN;
+    double *row = C + (int64_t)i * 16 * K + 4 * A;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int b = kPowB[q];
+#pragma unroll
+        for (int oi = 0; oi < 4; oi++) {
+            const double u = U[b * (E + 1) + kPowB[oi]];
+            row[oi * K + q] = u * gx;
+            row[(4 + oi) * K + q] = u * gy;
+            row[(8 + oi) * K + q] = u * gz;
+        }
+#pragma unroll
+        for (int op = 0; op < 3; op++)
+            row[(12 + op) * K + q] = W[b * E + op + 1];
+        row[15 * K + q] = 0.0;
+    }
+}
+
+int launch_pair_tc_f(cudaStream_t st, int n2, int nN, const double *f2, double *F)
+{
+    const int64_t total = (int64_t)n2 * nN;
+    if (total == 0)
+        return CUTC_OK;
+    pair_tc_f_kernel<<<ceil_div(total, 256), 256, 0, st>>>(n2, nN, f2, F);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    return CUTC_OK;
+}
+
+int launch_pair_tc_coef(cudaStream_t st, int i0, int n, int nN, const double *r1, const double *rn,
+                        double a_en, const double *coef, const int *exps, const int *term_off,
+                        double *C)
+{
+    const int64_t total = (int64_t)n * nN;
+    if (total == 0)
+        return CUTC_OK;
+    pair_tc_coef_kernel<<<ceil_div(total, 128), 128, 0, st>>>(i0, n, nN, r1, rn, a_en, coef,
+                                                              exps, term_off, C);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    return CUTC_OK;
 }
 
 __global__ void f64_to_df_kernel(double *x, int64_t n)

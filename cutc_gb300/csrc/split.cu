@@ -43,10 +43,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <cstdlib>
 #include <vector>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "digits.cuh"
+#include "pair.cuh"
+#include "pair_near.cuh"
 #include "products.cuh"
 #include "split.cuh"
 #include "tc.cuh"
@@ -340,6 +345,341 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                                         n % P.ncol_group;
                     double *dst = P.C + m + P.ldc * col;
                     *dst = P.accumulate ? *dst + val : val;
+                }
+            }
+        }
+    }
+
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == kMmaWarp)
+        tc::tmem_dealloc(tbase, kTmemCols);
+}
+
+
+// ---------------------------------------------------------------------------
+// Pair terms on the tensor cores (split form, Jastrow exponents in {0, 2, 3, 4})
+//
+// The nucleus sum of grad1 u(r1, r2) is, for fixed g12, the contraction
+//   V_c(r1, r2) = sum_k C[(r1, c)][k] F[r2][k],  k = 4 A + q over (nucleus, power of f2)
+// (pair_df.cu builds F and the 16 coefficient rows C per r1 point in FP64).  Here it
+// runs as a split contraction: A = the F slices (one 128-row tile of r2 points, all
+// of K, loaded once per CTA), B = the coefficient slices (N tiles of BN rows = BN/16
+// r1 points, streamed), one stacked-diagonal accumulator set per N tile in tensor
+// memory, double-buffered.  K = 4 n_nuc <= 80, so every diagonal sum is one chunk:
+// diagonals 0..2 are exact in FP32 ((d + 1) * 80 * 2^16 < 2^24), d >= 3 are 2^-27 and
+// below, where FP32 rounding is immaterial.
+//
+// The epilogue warps (lane = r2 point, one r1 point per warp) read the S diagonals
+// of the point's 16 columns, add them into double-float values (two_sum on the
+// three leading diagonals), release the accumulators, then finish the pair in
+// double-float exactly as pair_df_kernel does: g12 and its gradient, the powers of
+// g, -1/2 |grad u|^2, the FP64 path near e-e coalescence, the (hi, lo) G planes and
+// the G row maxima for the slicer.  Per pair that is about 800 FP32 operations
+// instead of 30 df multiply-adds (~450 operations) per nucleus.
+// ---------------------------------------------------------------------------
+
+struct PairTcParams {
+    int tiles_m, tiles_n, chunk;  // r2 tiles of 128 points, N tiles, N tiles per CTA
+    int Mpad, Npad;               // padded rows of the F and coefficient slices
+    const int *ea, *eb;           // their row exponents
+    PairDfArgs P;                 // geometry, near-coalescence path and outputs
+    int *err;
+};
+
+template <int S, int KB>
+struct PairTcCfg {
+    static constexpr int kBN = bn_for(S);            // 48: three r1 points per N tile
+    static constexpr int kPts = kBN / 16;
+    static constexpr int kEpiWarps = 4 * kPts;       // lane quarter x r1 point
+    static constexpr int kTmaWarp = kEpiWarps;
+    static constexpr int kMmaWarp = kEpiWarps + 1;
+    static constexpr int kThreads = (kEpiWarps + 2) * 32;
+    static constexpr int kASlice = kBM * kBK * 2;
+    static constexpr int kBSlice = kBN * kBK * 2;
+    static constexpr int kABytes = KB * S * kASlice;
+    static constexpr int kStages = 2;
+    static constexpr int kBStage = KB * S * kBSlice;
+    static constexpr int kBuf = kBN * S;             // tensor-memory columns per buffer
+    static constexpr int kSmem = kABytes + kStages * kBStage + 1024 + 256;
+    static_assert(kSmem <= 227 * 1024, "shared memory");
+    static_assert(2 * kBuf <= (int)kTmemCols, "accumulators exceed tensor memory");
+    static_assert(kBN * S <= 256, "instruction N exceeds 256");
+    static_assert(kBSlice % 512 == 0, "B slices must stack on 8-row swizzle atoms");
+};
+
+// x 2^e for the scale of a value of row exponents e (clamped to the float range)
+__device__ __forceinline__ float pow2f(int e)
+{
+    e = e < -126 ? -126 : (e > 127 ? 127 : e);
+    return __int_as_float((e + 127) << 23);
+}
+
+template <int S, int KB>
+__global__ void __launch_bounds__(PairTcCfg<S, KB>::kThreads, 1)
+pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+               const __grid_constant__ PairTcParams Q)
+{
+    using Cfg = PairTcCfg<S, KB>;
+    constexpr int D = S - 1, BN = Cfg::kBN;
+    constexpr int kEpiWarps = Cfg::kEpiWarps, kTmaWarp = Cfg::kTmaWarp, kMmaWarp = Cfg::kMmaWarp;
+    constexpr int kStages = Cfg::kStages;
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + Cfg::kABytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + kStages * Cfg::kBStage);
+    uint64_t *afull = bars;
+    uint64_t *full = bars + 1;
+    uint64_t *empty = full + kStages;
+    uint64_t *tfull = empty + kStages;
+    uint64_t *tempty = tfull + 2;
+    uint64_t *drain = tempty + 2;
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(drain + 1);
+    volatile int *s_abort = reinterpret_cast<volatile int *>(s_tmem + 1);
+
+    const PairDfArgs &P = Q.P;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = (int)(blockIdx.x % Q.tiles_m) * kBM;
+    const int t_begin = (int)(blockIdx.x / Q.tiles_m) * Q.chunk;
+    const int ntiles = min(Q.tiles_n, t_begin + Q.chunk) - t_begin;
+
+    if (threadIdx.x == 0) {
+        tc::mbar_init(tc::smem_u32(afull), 1);
+        for (int i = 0; i < kStages; i++) {
+            tc::mbar_init(tc::smem_u32(&full[i]), 1);
+            tc::mbar_init(tc::smem_u32(&empty[i]), 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            tc::mbar_init(tc::smem_u32(&tfull[i]), 1);
+            tc::mbar_init(tc::smem_u32(&tempty[i]), kEpiWarps);
+        }
+        tc::mbar_init(tc::smem_u32(drain), 1);
+        *s_abort = 0;
+        tc::fence_mbar_init();
+    }
+    if (warp == kMmaWarp) {
+        tc::tmem_alloc(tc::smem_u32(s_tmem), kTmemCols);
+        tc::tmem_relinquish();
+    }
+    if (warp == kTmaWarp && lane == 0) {
+        tc::tma_prefetch(&tmA);
+        tc::tma_prefetch(&tmB);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *s_tmem;
+
+    auto fail = [&](int code) {
+        *s_abort = 1;
+        atomicExch(Q.err, code);
+    };
+
+    if (warp == kTmaWarp) {
+        if (lane == 0) {
+            const uint32_t ab = tc::smem_u32(afull);
+            tc::mbar_arrive_expect_tx(ab, Cfg::kABytes);
+#pragma unroll
+            for (int kb = 0; kb < KB; kb++)
+#pragma unroll
+                for (int s = 0; s < S; s++)
+                    tc::tma_load_2d(tc::smem_u32(sA + (kb * S + s) * Cfg::kASlice), &tmA, kb * kBK,
+                                    s * Q.Mpad + m0, ab);
+            int issued = 0;
+            for (int q = 0; q < ntiles; q++) {
+                const int stage = q % kStages, round = q / kStages;
+                if (round > 0 &&
+                    !tc::mbar_wait(tc::smem_u32(&empty[stage]), (round - 1) & 1, s_abort)) {
+                    fail(11);
+                    break;
+                }
+                const uint32_t fb = tc::smem_u32(&full[stage]);
+                tc::mbar_arrive_expect_tx(fb, Cfg::kBStage);
+                uint8_t *st = sB + stage * Cfg::kBStage;
+                const int n0 = (t_begin + q) * BN;
+#pragma unroll
+                for (int kb = 0; kb < KB; kb++)
+#pragma unroll
+                    for (int t = 0; t < S; t++)
+                        tc::tma_load_2d(tc::smem_u32(st + (kb * S + t) * Cfg::kBSlice), &tmB,
+                                        kb * kBK, t * Q.Npad + n0, fb);
+                issued = q + 1;
+            }
+            // let the copies still in flight land before the CTA goes away
+            tc::mbar_wait(ab, 0, nullptr);
+            if (*s_abort) {
+                for (int q = max(0, issued - kStages); q < issued; q++)
+                    tc::mbar_wait(tc::smem_u32(&full[q % kStages]), (q / kStages) & 1, nullptr);
+            }
+        }
+    } else if (warp == kMmaWarp) {
+        if (lane == 0) {
+            bool ok = tc::mbar_wait(tc::smem_u32(afull), 0, s_abort);
+            if (!ok)
+                fail(12);
+            for (int q = 0; q < ntiles && ok; q++) {
+                const int b = q & 1, stage = q % kStages;
+                if (q >= 2 && !tc::mbar_wait(tc::smem_u32(&tempty[b]), ((q >> 1) - 1) & 1, s_abort)) {
+                    fail(13);
+                    break;
+                }
+                if (!tc::mbar_wait(tc::smem_u32(&full[stage]), (q / kStages) & 1, s_abort)) {
+                    fail(14);
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t sb0 = tc::smem_u32(sB + stage * Cfg::kBStage);
+                const uint32_t sa0 = tc::smem_u32(sA);
+                bool first = true;
+#pragma unroll
+                for (int kb = 0; kb < KB; kb++) {
+#pragma unroll
+                    for (int k16 = 0; k16 < kBK / 16; k16++) {
+                        const uint64_t bd =
+                            tc::smem_desc_sw64(sb0 + kb * S * Cfg::kBSlice + k16 * 32);
+#pragma unroll
+                        for (int s = 0; s < S; s++) {
+                            // a_s x [b_0 .. b_{D-s}] -> diagonals s .. D
+                            const uint32_t idesc = tc::idesc_bf16_f32(kBM, BN * (D + 1 - s));
+                            const uint64_t ad = tc::smem_desc_sw64(
+                                sa0 + (kb * S + s) * Cfg::kASlice + k16 * 32);
+                            tc::mma_bf16(tbase + (uint32_t)(Cfg::kBuf * b + BN * s), ad, bd,
+                                         idesc, first ? 0u : 1u);
+                            first = false;
+                        }
+                    }
+                }
+                tc::mma_commit(tc::smem_u32(&empty[stage]));
+                tc::mma_commit(tc::smem_u32(&tfull[b]));
+            }
+            tc::mma_commit(tc::smem_u32(drain));
+            if (!tc::mbar_wait(tc::smem_u32(drain), 0, nullptr))
+                fail(15);
+        }
+    } else {
+        // ---- epilogue: one r1 point of each N tile, 32 r2 points ---------------------
+        const int quarter = warp & 3, pt = warp >> 2;
+        const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
+        const int j = m0 + quarter * 32 + lane;
+        const bool jok = j < P.n2;
+        const int jc = jok ? j : 0;
+        const float2 x2 = P.r2d[jc], y2 = P.r2d[P.n2 + jc], z2 = P.r2d[2 * (int64_t)P.n2 + jc];
+        const float sa = pow2f(Q.ea[jc]);  // F rows: 2^1 (f^0 = 1 is the row maximum)
+        const df::D a = df::make(P.a_ee_hi, P.a_ee_lo);
+        for (int q = 0; q < ntiles; q++) {
+            const int b = q & 1;
+            if (!tc::mbar_wait(tc::smem_u32(&tfull[b]), (q >> 1) & 1, s_abort)) {
+                fail(16);
+                break;
+            }
+            tc::fence_after_sync();
+            // the point's 16 columns on each diagonal, added into (hi, lo)
+            float h[16], l[16];
+            {
+                const uint32_t cb = tbase + lane_off + (uint32_t)(Cfg::kBuf * b + 16 * pt);
+                float v[16];
+                tc::tmem_ld16(cb, v);
+#pragma unroll
+                for (int c = 0; c < 16; c++) {
+                    h[c] = v[c];
+                    l[c] = 0.f;
+                }
+#pragma unroll
+                for (int d = 1; d <= D; d++) {
+                    tc::tmem_ld16(cb + (uint32_t)(BN * d), v);
+#pragma unroll
+                    for (int c = 0; c < 16; c++) {
+                        if (d <= 2) {
+                            const df::D t = df::two_sum(h[c], v[c]);
+                            h[c] = t.hi;
+                            l[c] = __fadd_rn(l[c], t.lo);
+                        } else {
+                            l[c] = __fadd_rn(l[c], v[c]);
+                        }
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0)
+                tc::mbar_arrive(tc::smem_u32(&tempty[b]));
+
+            const int i = (t_begin + q) * Cfg::kPts + pt;  // r1 row of the tile
+            if (i >= P.n1b)
+                continue;
+            // V_c = 2^(ea + eb_c) (h + l), renormalised
+            df::D V[15];
+            const int *ebr = Q.eb + (int64_t)i * 16;
+#pragma unroll
+            for (int c = 0; c < 15; c++) {
+                const float sc = sa * pow2f(ebr[c]);
+                V[c] = df::fast_two_sum(h[c] * sc, l[c] * sc);
+            }
+            const int64_t o = (int64_t)i * P.ldg + j;
+            float2 w4[4];
+            if (jok) {
+                const double *r1p = P.r1 + 3 * (int64_t)(P.i0 + i);
+                const df::D x1 = df::from_double(r1p[0]), y1 = df::from_double(r1p[1]),
+                            z1 = df::from_double(r1p[2]);
+                const df::D dx = df::sub(x1, df::make(x2.x, x2.y));
+                const df::D dy = df::sub(y1, df::make(y2.x, y2.y));
+                const df::D dz = df::sub(z1, df::make(z2.x, z2.y));
+                const df::D d2 = df::add(df::add(df::sqr(dx), df::sqr(dy)), df::sqr(dz));
+                if (d2.hi < kNearPairR2) {
+                    double v[4];
+                    pair_fp64_single(P, i, j, v);
+                    for (int c = 0; c < 4; c++) {
+                        const df::D w = df::from_double(v[c]);
+                        w4[c] = make_float2(w.hi, w.lo);
+                    }
+                } else {
+                    const df::D rd = df::sqrt(d2);
+                    const df::D ar = df::mul(rd, a);
+                    const df::D t = df::recip(df::add_f(ar, 1.0f));
+                    const df::D g = df::mul(ar, t);
+                    const df::D sg = df::mul(df::mul(df::sqr(t), a), df::recip(rd));
+                    const df::D gx = df::mul(sg, dx), gy = df::mul(sg, dy), gz = df::mul(sg, dz);
+                    const df::D g2 = df::sqr(g);
+                    // sum_o g^o V_o, o = 0, 2, 3, 4
+                    auto poly = [&](int c0) {
+                        return df::fma(df::fma(df::fma(V[c0 + 3], g, V[c0 + 2]), g, V[c0 + 1]), g2,
+                                       V[c0]);
+                    };
+                    df::D ux = poly(0), uy = poly(4), uz = poly(8);
+                    const df::D dudg = df::mul(df::fma(df::fma(V[14], g, V[13]), g, V[12]), g);
+                    ux = df::fma(dudg, gx, ux);
+                    uy = df::fma(dudg, gy, uy);
+                    uz = df::fma(dudg, gz, uz);
+                    const df::D n2v = df::add(df::add(df::sqr(ux), df::sqr(uy)), df::sqr(uz));
+                    const df::D lv = df::mul_f(n2v, -0.5f);
+                    w4[0] = make_float2(ux.hi, ux.lo);
+                    w4[1] = make_float2(uy.hi, uy.lo);
+                    w4[2] = make_float2(uz.hi, uz.lo);
+                    w4[3] = make_float2(lv.hi, lv.lo);
+                }
+#pragma unroll
+                for (int c = 0; c < 4; c++)
+                    P.G[o + c * P.plane] = w4[c];
+            }
+            if (P.rmax) {
+                // row maxima for the slicer from the float bits (as pair_df_kernel)
+                const unsigned mask = __ballot_sync(0xffffffffu, jok);
+                if (jok) {
+                    const bool leader = lane == __ffs(mask) - 1;
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const unsigned fb = __float_as_uint(w4[c].x) & 0x7fffffffu;
+                        const unsigned ef = fb >> 23;
+                        const unsigned hw = fb == 0u ? 0u
+                                          : ef == 0u ? (897u << 20)
+                                                     : ((ef + 896u) << 20) | ((fb & 0x7fffffu) >> 3);
+                        const unsigned m = __reduce_max_sync(mask, hw);
+                        if (leader && m)
+                            atomicMax(&P.rmax[(int64_t)c * P.n1b + i], (unsigned long long)m << 32);
+                    }
                 }
             }
         }
@@ -732,6 +1072,7 @@ static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alph
 enum SplitSlot {
     SS_PAIRS_SYM = 0, SS_PAIRS_ANTI = 1, SS_ERR = 2,
     SS_AX = 3, SS_BX = 6, SS_AH = 9, SS_AN = 12, SS_BH = 15, SS_BN = 18,
+    SS_AF = 21, SS_BC = 24, SS_F64 = 27, SS_C64 = 28,
 };
 
 
@@ -873,6 +1214,121 @@ int split_int2e_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp
     } else {
         E->tag_i = 0;
     }
+    return CUTC_OK;
+}
+
+// ---- pair terms on the tensor cores -------------------------------------------------
+
+constexpr int kPairTcSlices = 5;   // the slice count the kernel is built for
+constexpr int kPairTcMaxNuc = 20;  // K = 4 n_nuc <= 80 keeps diagonals 0..2 exact
+
+bool split_pair_tc_ok(const Request &R, const int *exps, int n_terms)
+{
+    return R.precision == CUTC_SPLIT_BF16 && !R.pair_fp64 && R.n_slices == kPairTcSlices &&
+           R.nN <= kPairTcMaxNuc && pair_df_sparse(exps, n_terms) && !getenv("CUTC_PAIR_DF") &&
+           !getenv("CUTC_PAIR_DENSE");
+}
+
+size_t split_pair_fixed_bytes(const Request &R)
+{
+    const int64_t K = 4 * (int64_t)R.nN;
+    return (size_t)R.n2 * K * 8 + 2 * (size_t)R.n_slices * round_up(R.n2, kBM) * round_up(K, kBK);
+}
+
+size_t split_pair_row_bytes(const Request &R)
+{
+    const int64_t K = 4 * (int64_t)R.nN;
+    return 16 * (size_t)K * 8 + 2 * (size_t)R.n_slices * 16 * round_up(K, kBK) + 64;
+}
+
+int split_pair_prepare(Engine *E, const Request &R, cudaStream_t st, const double *f2,
+                       int64_t n1t, SplitPlan &sp)
+{
+    Workspace &W = E->ws;
+    const int slot0 = sp.slot0;
+    const int64_t K = 4 * (int64_t)R.nN;
+    void *p;
+    CUTC_TRY(W.get(slot0 + SS_F64, (size_t)R.n2 * K * 8, &p));
+    sp.Fd = (double *)p;
+    CUTC_TRY(W.get(slot0 + SS_C64, (size_t)16 * n1t * K * 8, &p));
+    sp.Cd = (double *)p;
+    CUTC_TRY(alloc_operand(W, slot0 + SS_AF, kPairTcSlices, R.n2, kBM, K, sp.AF));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BC, kPairTcSlices, (int)(16 * n1t),
+                           bn_for(kPairTcSlices), K, sp.BC));
+    CUTC_TRY(launch_pair_tc_f(st, R.n2, R.nN, f2, sp.Fd));
+    note_launches(1);
+    SrcDense src{sp.Fd, K};
+    CUTC_TRY((slice_rows<kPairTcSlices, SrcDense>(st, src, sp.AF)));
+    sp.pair_tc = true;
+    return CUTC_OK;
+}
+
+template <int S, int KB>
+static int launch_pair_tc_kernel(cudaStream_t st, const CUtensorMap &ta, const CUtensorMap &tb,
+                                 PairTcParams Q, int n_sm)
+{
+    using Cfg = PairTcCfg<S, KB>;
+    static std::atomic<unsigned long long> attr_done{0};
+    const unsigned long long bit = current_device_bit();
+    if (!(attr_done.load() & bit)) {
+        CUTC_CUDA_TRY(cudaFuncSetAttribute(pair_tc_kernel<S, KB>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem));
+        attr_done.fetch_or(bit);
+    }
+    // about eight CTAs per SM, each walking a run of N tiles with its F tile resident
+    const int64_t want = 8 * (int64_t)n_sm;
+    const int64_t chunks = std::max<int64_t>(
+        1, std::min<int64_t>(Q.tiles_n, (want + Q.tiles_m - 1) / Q.tiles_m));
+    Q.chunk = (int)((Q.tiles_n + chunks - 1) / chunks);
+    const int64_t grid = (int64_t)Q.tiles_m * ((Q.tiles_n + Q.chunk - 1) / Q.chunk);
+    if (grid > INT32_MAX) {
+        cutc_set_error(CUTC_ERR_INVALID, "pair grid of %lld CTAs", (long long)grid);
+        return CUTC_ERR_INVALID;
+    }
+    pair_tc_kernel<S, KB><<<(unsigned)grid, Cfg::kThreads, Cfg::kSmem, st>>>(ta, tb, Q);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    return CUTC_OK;
+}
+
+int split_pair_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
+                    const PairDfArgs &P, const double *rn, double a_en)
+{
+    constexpr int S = kPairTcSlices;
+    constexpr int BN = bn_for(S);
+    (void)R;
+    if (P.n1b <= 0 || P.n2 <= 0)
+        return CUTC_OK;
+    const int64_t K = 4 * (int64_t)P.nN;
+    CUTC_TRY(launch_pair_tc_coef(st, P.i0, P.n1b, P.nN, P.r1, rn, a_en, P.coef, P.exps,
+                                 P.term_off, sp.Cd));
+    Operand B = sp.BC;
+    B.M = 16 * P.n1b;
+    B.Mpad = (int)round_up(B.M, BN);
+    SrcDense src{sp.Cd, K};
+    CUTC_TRY((slice_rows<S, SrcDense>(st, src, B)));
+    CUtensorMap ta, tb;
+    CUTC_TRY(make_tmap(&ta, sp.AF.sl, (int64_t)S * sp.AF.Mpad, sp.AF.Kpad, kBM));
+    CUTC_TRY(make_tmap(&tb, B.sl, (int64_t)S * B.Mpad, B.Kpad, BN));
+    PairTcParams Q;
+    Q.tiles_m = sp.AF.Mpad / kBM;
+    Q.tiles_n = B.Mpad / BN;
+    Q.chunk = 1;
+    Q.Mpad = sp.AF.Mpad;
+    Q.Npad = B.Mpad;
+    Q.ea = sp.AF.ex;
+    Q.eb = B.ex;
+    Q.P = P;
+    Q.err = sp.err;
+    const int KB = (int)(sp.AF.Kpad / kBK);
+    switch (KB) {
+    case 1: CUTC_TRY((launch_pair_tc_kernel<S, 1>(st, ta, tb, Q, E->n_sm))); break;
+    case 2: CUTC_TRY((launch_pair_tc_kernel<S, 2>(st, ta, tb, Q, E->n_sm))); break;
+    case 3: CUTC_TRY((launch_pair_tc_kernel<S, 3>(st, ta, tb, Q, E->n_sm))); break;
+    default:
+        cutc_set_error(CUTC_ERR_INVALID, "pair contraction of K = %lld", (long long)K);
+        return CUTC_ERR_INVALID;
+    }
+    note_launches(2);
     return CUTC_OK;
 }
 

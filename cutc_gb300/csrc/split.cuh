@@ -26,6 +26,11 @@ struct SplitPlan {
     int64_t n1t = 0;
     Operand AX;                        // P slices: X-build A operand
     Operand BX;                        // G-tile slices: X-build B operand
+    // pair terms on the tensor cores: F slices (powers of f2 on r2), the tile's
+    // coefficient slices, and their FP64 sources
+    bool pair_tc = false;
+    Operand AF, BC;
+    double *Fd = nullptr, *Cd = nullptr;
     int2 *pairs_sym = nullptr;         // (a, b), a >= b, in tri_index order
     int2 *pairs_anti = nullptr;        // (a, b), a > b, in stri_index order
     int *err = nullptr;                // device flag set by a bounded wait that gave up
@@ -55,6 +60,22 @@ int split_x_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp, co
 int split_int2e_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
                      const double *wr1, const double *aos1, int64_t ld1, int nb, const double *Xt,
                      double *H, double *N, bool first);
+// The pair terms of a split-form build on the tensor cores: applicable when every
+// Jastrow exponent is 0, 2, 3 or 4, n_nuc <= 20, the build uses 5 slices and neither
+// FP64 pair terms nor CUTC_PAIR_DF / CUTC_PAIR_DENSE (the double-float kernels) is asked
+// for.
+bool split_pair_tc_ok(const Request &R, const int *exps, int n_terms);
+// Builds the F operand (powers of f2 on the r2 points; f2 is [n_nuc][n2] FP64) once per
+// build and reserves the coefficient operand for tiles of up to n1t rows.
+int split_pair_prepare(Engine *E, const Request &R, cudaStream_t st, const double *f2,
+                       int64_t n1t, SplitPlan &sp);
+// The pair planes G of one r1 tile (P: the tile's rows, outputs and near-coalescence
+// data, as for launch_pair_df; its rmax must be zeroed).
+int split_pair_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
+                    const PairDfArgs &P, const double *rn, double a_en);
+// Device bytes of the tensor-core pair operands: fixed (F) and per r1 row of a tile.
+size_t split_pair_fixed_bytes(const Request &R);
+size_t split_pair_row_bytes(const Request &R);
 // Reports a bounded wait that gave up in any of the launches (synchronises).
 int split_check(cudaStream_t st, SplitPlan &sp);
 // C[m + ldc n] = sum_k A[m K + k] B[n K + k] through the split form (device arrays)

@@ -96,3 +96,23 @@ def test_sparse_power_pair_kernel_matches_general(monkeypatch):
     assert oracle.rel_err(I1, I2)["max"] < 1e-12
     Xo, Io = oracle.cutc_int(p)
     _check(X1[:3], I1, Xo, Io)
+
+
+@pytest.mark.parametrize("n_nuc,coalesce", [(6, False), (3, True), (20, False), (1, False)])
+def test_tensor_core_pair_terms_match_double_float_kernel(monkeypatch, n_nuc, coalesce):
+    """With exponents in {0, 2, 3, 4} and up to 20 nuclei the split form's pair terms
+    run on the tensor cores (a contraction over nucleus and power of f2, K = 4 n_nuc);
+    CUTC_PAIR_DF selects the double-float kernel.  Both against each other and the
+    oracle, including e-e and e-n coalescence (the FP64 path of the epilogue) and
+    K = 80 (20 nuclei), the largest contraction whose leading diagonals stay exact."""
+    p = synth.make_problem(n_nuc=n_nuc, n_ao=8, n_grid1=260, n_grid2=900, size_bh=9,
+                           seed=70 + n_nuc, a_en=0.9, a_ee=1.2, box=1.5 + 0.4 * n_nuc)
+    if coalesce:
+        p = synth.add_coalescence(p)
+    X1, I1 = cg.build_integrals(p, cg.SPLIT_BF16, x_components=4)
+    monkeypatch.setenv("CUTC_PAIR_DF", "1")
+    X2, I2 = cg.build_integrals(p, cg.SPLIT_BF16, x_components=4)
+    assert oracle.rel_err(X1, X2)["max"] < 1e-12
+    assert oracle.rel_err(I1, I2)["max"] < 1e-12
+    Xo, Io = oracle.cutc_int(p)
+    _check(X1[:3], I1, Xo, Io)
