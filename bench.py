@@ -1107,10 +1107,10 @@ def run_kernel(args):
                        note="call time includes slicing both operands")
         print(json.dumps(rec))
     elif k == "pair":
-        # a molecule with the medium workload's nuclei and Jastrow terms but few AOs (the
-        # pair terms do not depend on n_ao), so the device holds a few GB
-        p = synth.make_problem(n_nuc=args.n_nuc, n_ao=40, n_grid1=args.n1, n_grid2=args.n2,
-                               size_bh=args.terms, seed=2002, box=6.0)
+        # a molecule with the medium workload's nuclei and Jastrow terms; by default few AOs
+        # (the pair terms do not depend on n_ao), so the device holds a few GB
+        p = synth.make_problem(n_nuc=args.n_nuc, n_ao=args.n_ao, n_grid1=args.n1,
+                               n_grid2=args.n2, size_bh=args.terms, seed=2002, box=6.0)
         pair_ms = []
         for _ in range(args.reps):
             _, _, st = cg.build_integrals(p, cg.SPLIT_BF16, with_stats=True)
@@ -1243,6 +1243,7 @@ def main(argv=None):
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--rows", type=int, default=256)
     ap.add_argument("--n-nuc", type=int, default=10)
+    ap.add_argument("--n-ao", type=int, default=40, help="pair micro-benchmark: AOs of the molecule")
     ap.add_argument("--terms", type=int, default=13)
     ap.add_argument("--n1", type=int, default=1024)
     ap.add_argument("--n2", type=int, default=80000)

@@ -68,11 +68,12 @@ int launch_pair_df(cudaStream_t st, const PairDfArgs &P, int E, bool sparse, con
 
 // Operands of the tensor-core pair terms (exponents in {0, 2, 3, 4}), FP64: the powers
 // F[j * 4 nN + 4 A + q] = f2_A(r2_j)^b_q (b = 0, 2, 3, 4) and, for r1 rows [i0, i0 + n),
-// the 16 coefficient rows C[((i 16 + c) 4 nN) + 4 A + q] of each point.
+// the 16 coefficient rows C[((i 16 + c) 4 nN) + 4 A + q] of each point, with the points
+// themselves in double-float, r1d[3 i + c].
 int launch_pair_tc_f(cudaStream_t st, int n2, int nN, const double *f2, double *F);
 int launch_pair_tc_coef(cudaStream_t st, int i0, int n, int nN, const double *r1, const double *rn,
                         double a_en, const double *coef, const int *exps, const int *term_off,
-                        double *C);
+                        double *C, float2 *r1d);
 
 int launch_r1_terms(cudaStream_t st, int i0, int n, int nN, const double *r1, const double *rn,
                     double a, NucTerm *t1);

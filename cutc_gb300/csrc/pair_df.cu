@@ -305,12 +305,13 @@ __global__ void pair_tc_f_kernel(int n2, int nN, const double *__restrict__ f2,
 }
 
 // C[((i 16 + c) 4 nN) + 4 A + q] for rows i of the tile, FP64; the polynomial
-// coefficients U, W are formed as in r1_poly_kernel<4>.
+// coefficients U, W are formed as in r1_poly_kernel<4>.  Also the tile's r1 points in
+// double-float, r1d[3 i + c].
 __global__ void pair_tc_coef_kernel(int i0, int n, int nN, const double *__restrict__ r1,
                                     const double *__restrict__ rn, double a_en,
                                     const double *__restrict__ tcoef,
                                     const int *__restrict__ texps, const int *__restrict__ toff,
-                                    double *__restrict__ C)
+                                    double *__restrict__ C, float2 *__restrict__ r1d)
 {
     constexpr int E = 4;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -318,6 +319,11 @@ __global__ void pair_tc_coef_kernel(int i0, int n, int nN, const double *__restr
         return;
     const int i = (int)(idx / nN), A = (int)(idx % nN);
     const double *p = r1 + 3 * (int64_t)(i0 + i);
+    if (A == 0)
+        for (int c = 0; c < 3; c++) {  // the point in double-float, for the pair epilogue
+            const df::D v = df::from_double(p[c]);
+            r1d[3 * (int64_t)i + c] = make_float2(v.hi, v.lo);
+        }
     const double dx = p[0] - rn[3 * A], dy = p[1] - rn[3 * A + 1], dz = p[2] - rn[3 * A + 2];
     const double d2 = dx * dx + dy * dy + dz * dz;
     double f = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
@@ -383,13 +389,13 @@ int launch_pair_tc_f(cudaStream_t st, int n2, int nN, const double *f2, double *
 
 int launch_pair_tc_coef(cudaStream_t st, int i0, int n, int nN, const double *r1, const double *rn,
                         double a_en, const double *coef, const int *exps, const int *term_off,
-                        double *C)
+                        double *C, float2 *r1d)
 {
     const int64_t total = (int64_t)n * nN;
     if (total == 0)
         return CUTC_OK;
     pair_tc_coef_kernel<<<ceil_div(total, 128), 128, 0, st>>>(i0, n, nN, r1, rn, a_en, coef,
-                                                              exps, term_off, C);
+                                                              exps, term_off, C, r1d);
     CUTC_CUDA_TRY(cudaGetLastError());
     return CUTC_OK;
 }

@@ -372,9 +372,9 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 // below, where FP32 rounding is immaterial.
 //
 // The epilogue warps (lane = r2 point, one r1 point per warp) read the S diagonals
-// of the point's 16 columns, add them into double-float values (two_sum on the
-// three leading diagonals), release the accumulators, then finish the pair in
-// double-float exactly as pair_df_kernel does: g12 and its gradient, the powers of
+// of the point's 16 columns, add them exactly on fixed grids into double-float
+// values, release the accumulators, then finish the pair in double-float exactly as
+// pair_df_kernel does: g12 and its gradient, the powers of
 // g, -1/2 |grad u|^2, the FP64 path near e-e coalescence, the (hi, lo) G planes and
 // the G row maxima for the slicer.  Per pair that is about 800 FP32 operations
 // instead of 30 df multiply-adds (~450 operations) per nucleus.
@@ -383,10 +383,22 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 struct PairTcParams {
     int tiles_m, tiles_n, chunk;  // r2 tiles of 128 points, N tiles, N tiles per CTA
     int Mpad, Npad;               // padded rows of the F and coefficient slices
-    const int *ea, *eb;           // their row exponents
+    const int *ea;                // row exponents of the F slices
+    const float *bscale;          // 2^(row exponent) of each coefficient row
+    const float2 *r1d;            // the tile's r1 points in double-float, [3 i + c]
     PairDfArgs P;                 // geometry, near-coalescence path and outputs
     int *err;
 };
+
+// bscale[r] = 2^ex[r] as a float
+__global__ void exp_scale_kernel(const int *__restrict__ ex, int rows, float *__restrict__ bscale)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < rows) {
+        const int e = max(-126, min(127, ex[r]));
+        bscale[r] = __int_as_float((e + 127) << 23);
+    }
+}
 
 template <int S, int KB>
 struct PairTcCfg {
@@ -576,28 +588,41 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 break;
             }
             tc::fence_after_sync();
-            // the point's 16 columns on each diagonal, added into (hi, lo)
-            float h[16], l[16];
+            // The point's 16 columns on each diagonal, summed exactly on grids.  In units of
+            // the row scales every diagonal sum D_d is a multiple of 2^(-16-9d) and |D_0| <= K:
+            //   H  = D_0 + D_1 rounded to multiples of 2^-16      (exact: below 2^7 there)
+            //   L  = the rest of D_1 + D_2 rounded to 2^-25         (exact: below 2^-8 there)
+            //   L2 = the rest of D_2 + D_3 + ... (FP32; below 2^-18, so off by < 2^-42)
+            // Two columns share each packed f32x2 operation.
+            uint64_t H[8], L[8], L2[8];
             {
                 const uint32_t cb = tbase + lane_off + (uint32_t)(Cfg::kBuf * b + 16 * pt);
+                const uint64_t C16 = tc::f2_pack(__float_as_uint(192.0f), __float_as_uint(192.0f));
+                const uint64_t C25 = tc::f2_pack(__float_as_uint(0.375f), __float_as_uint(0.375f));
                 float v[16];
                 tc::tmem_ld16(cb, v);
 #pragma unroll
-                for (int c = 0; c < 16; c++) {
-                    h[c] = v[c];
-                    l[c] = 0.f;
+                for (int k = 0; k < 8; k++) {
+                    H[k] = tc::f2_pack(__float_as_uint(v[2 * k]), __float_as_uint(v[2 * k + 1]));
+                    L[k] = L2[k] = 0ull;
                 }
 #pragma unroll
                 for (int d = 1; d <= D; d++) {
                     tc::tmem_ld16(cb + (uint32_t)(BN * d), v);
 #pragma unroll
-                    for (int c = 0; c < 16; c++) {
-                        if (d <= 2) {
-                            const df::D t = df::two_sum(h[c], v[c]);
-                            h[c] = t.hi;
-                            l[c] = __fadd_rn(l[c], t.lo);
+                    for (int k = 0; k < 8; k++) {
+                        const uint64_t x =
+                            tc::f2_pack(__float_as_uint(v[2 * k]), __float_as_uint(v[2 * k + 1]));
+                        if (d == 1) {
+                            const uint64_t hh = tc::f2_sub(tc::f2_add(x, C16), C16);
+                            H[k] = tc::f2_add(H[k], hh);
+                            L[k] = tc::f2_sub(x, hh);
+                        } else if (d == 2) {
+                            const uint64_t hh = tc::f2_sub(tc::f2_add(x, C25), C25);
+                            L[k] = tc::f2_add(L[k], hh);
+                            L2[k] = tc::f2_sub(x, hh);
                         } else {
-                            l[c] = __fadd_rn(l[c], v[c]);
+                            L2[k] = tc::f2_add(L2[k], x);
                         }
                     }
                 }
@@ -610,56 +635,71 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             const int i = (t_begin + q) * Cfg::kPts + pt;  // r1 row of the tile
             if (i >= P.n1b)
                 continue;
-            // V_c = 2^(ea + eb_c) (h + l), renormalised
-            df::D V[15];
-            const int *ebr = Q.eb + (int64_t)i * 16;
+            // V_c = 2^(ea + eb_c) ((H + L) + L2): TwoSum of H and L, then the rest
+            df::D V[16];
+            const float *scr = Q.bscale + (int64_t)i * 16;
 #pragma unroll
-            for (int c = 0; c < 15; c++) {
-                const float sc = sa * pow2f(ebr[c]);
-                V[c] = df::fast_two_sum(h[c] * sc, l[c] * sc);
+            for (int k = 0; k < 8; k++) {
+                const uint64_t sm = tc::f2_add(H[k], L[k]);
+                const uint64_t bb = tc::f2_sub(sm, H[k]);
+                uint64_t e = tc::f2_add(tc::f2_sub(H[k], tc::f2_sub(sm, bb)), tc::f2_sub(L[k], bb));
+                e = tc::f2_add(e, L2[k]);
+                const uint64_t sc = tc::f2_pack(__float_as_uint(sa * scr[2 * k]),
+                                                __float_as_uint(sa * scr[2 * k + 1]));
+                const uint64_t hs = tc::f2_mul(sm, sc), ls = tc::f2_mul(e, sc);
+                V[2 * k] = df::make(tc::f2_lo(hs), tc::f2_lo(ls));
+                V[2 * k + 1] = df::make(tc::f2_hi(hs), tc::f2_hi(ls));
             }
             const int64_t o = (int64_t)i * P.ldg + j;
             float2 w4[4];
             if (jok) {
-                const double *r1p = P.r1 + 3 * (int64_t)(P.i0 + i);
-                const df::D x1 = df::from_double(r1p[0]), y1 = df::from_double(r1p[1]),
-                            z1 = df::from_double(r1p[2]);
-                const df::D dx = df::sub(x1, df::make(x2.x, x2.y));
-                const df::D dy = df::sub(y1, df::make(y2.x, y2.y));
-                const df::D dz = df::sub(z1, df::make(z2.x, z2.y));
-                const df::D d2 = df::add(df::add(df::sqr(dx), df::sqr(dy)), df::sqr(dz));
+                const float2 *r1p = Q.r1d + 3 * (int64_t)i;
+                const float2 r1x = r1p[0], r1y = r1p[1], r1z = r1p[2];
+                df::D dx = df::sub(df::make(r1x.x, r1x.y), df::make(x2.x, x2.y));
+                df::D dy = df::sub(df::make(r1y.x, r1y.y), df::make(y2.x, y2.y));
+                df::D dz = df::sub(df::make(r1z.x, r1z.y), df::make(z2.x, z2.y));
+                df::D d2 = df::add(df::add(df::sqr(dx), df::sqr(dy)), df::sqr(dz));
+                bool coalesced = false;
                 if (d2.hi < kNearPairR2) {
-                    double v[4];
-                    pair_fp64_single(P, i, j, v);
-                    for (int c = 0; c < 4; c++) {
-                        const df::D w = df::from_double(v[c]);
-                        w4[c] = make_float2(w.hi, w.lo);
-                    }
-                } else {
+                    // near e-e coalescence the differences are taken in FP64, where they are
+                    // exact (the coordinates' double-float forms keep only 48 bits); only g12
+                    // and its gradient depend on them, so the rest stays as it is.  The
+                    // reference's own guard, r12^2 <= 1e-15 (src/jast_bh.cu:143), gives g = 0.
+                    const double *a1 = P.r1 + 3 * (int64_t)(P.i0 + i);
+                    const double *a2 = P.r2 + 3 * (int64_t)j;
+                    const double ex = a1[0] - a2[0], ey = a1[1] - a2[1], ez = a1[2] - a2[2];
+                    dx = df::from_double(ex);
+                    dy = df::from_double(ey);
+                    dz = df::from_double(ez);
+                    d2 = df::add(df::add(df::sqr(dx), df::sqr(dy)), df::sqr(dz));
+                    coalesced = !(ex * ex + ey * ey + ez * ez > 1e-15);
+                }
+                df::D g = {0.f, 0.f}, gx = {0.f, 0.f}, gy = {0.f, 0.f}, gz = {0.f, 0.f};
+                if (!coalesced) {
                     const df::D rd = df::sqrt(d2);
                     const df::D ar = df::mul(rd, a);
                     const df::D t = df::recip(df::add_f(ar, 1.0f));
-                    const df::D g = df::mul(ar, t);
+                    g = df::mul(ar, t);
                     const df::D sg = df::mul(df::mul(df::sqr(t), a), df::recip(rd));
-                    const df::D gx = df::mul(sg, dx), gy = df::mul(sg, dy), gz = df::mul(sg, dz);
-                    const df::D g2 = df::sqr(g);
-                    // sum_o g^o V_o, o = 0, 2, 3, 4
-                    auto poly = [&](int c0) {
-                        return df::fma(df::fma(df::fma(V[c0 + 3], g, V[c0 + 2]), g, V[c0 + 1]), g2,
-                                       V[c0]);
-                    };
-                    df::D ux = poly(0), uy = poly(4), uz = poly(8);
-                    const df::D dudg = df::mul(df::fma(df::fma(V[14], g, V[13]), g, V[12]), g);
-                    ux = df::fma(dudg, gx, ux);
-                    uy = df::fma(dudg, gy, uy);
-                    uz = df::fma(dudg, gz, uz);
-                    const df::D n2v = df::add(df::add(df::sqr(ux), df::sqr(uy)), df::sqr(uz));
-                    const df::D lv = df::mul_f(n2v, -0.5f);
-                    w4[0] = make_float2(ux.hi, ux.lo);
-                    w4[1] = make_float2(uy.hi, uy.lo);
-                    w4[2] = make_float2(uz.hi, uz.lo);
-                    w4[3] = make_float2(lv.hi, lv.lo);
+                    gx = df::mul(sg, dx);
+                    gy = df::mul(sg, dy);
+                    gz = df::mul(sg, dz);
                 }
+                const df::D g2 = df::sqr(g);
+                // sum_o g^o V_o, o = 0, 2, 3, 4
+                df::D ux = df::fma(df::fma(df::fma(V[3], g, V[2]), g, V[1]), g2, V[0]);
+                df::D uy = df::fma(df::fma(df::fma(V[7], g, V[6]), g, V[5]), g2, V[4]);
+                df::D uz = df::fma(df::fma(df::fma(V[11], g, V[10]), g, V[9]), g2, V[8]);
+                const df::D dudg = df::mul(df::fma(df::fma(V[14], g, V[13]), g, V[12]), g);
+                ux = df::fma(dudg, gx, ux);
+                uy = df::fma(dudg, gy, uy);
+                uz = df::fma(dudg, gz, uz);
+                const df::D n2v = df::add(df::add(df::sqr(ux), df::sqr(uy)), df::sqr(uz));
+                const df::D lv = df::mul_f(n2v, -0.5f);
+                w4[0] = make_float2(ux.hi, ux.lo);
+                w4[1] = make_float2(uy.hi, uy.lo);
+                w4[2] = make_float2(uz.hi, uz.lo);
+                w4[3] = make_float2(lv.hi, lv.lo);
 #pragma unroll
                 for (int c = 0; c < 4; c++)
                     P.G[o + c * P.plane] = w4[c];
@@ -1072,7 +1112,7 @@ static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alph
 enum SplitSlot {
     SS_PAIRS_SYM = 0, SS_PAIRS_ANTI = 1, SS_ERR = 2,
     SS_AX = 3, SS_BX = 6, SS_AH = 9, SS_AN = 12, SS_BH = 15, SS_BN = 18,
-    SS_AF = 21, SS_BC = 24, SS_F64 = 27, SS_C64 = 28,
+    SS_AF = 21, SS_BC = 24, SS_F64 = 27, SS_C64 = 28, SS_R1D = 29, SS_BSCALE = 30,
 };
 
 
@@ -1238,7 +1278,8 @@ size_t split_pair_fixed_bytes(const Request &R)
 size_t split_pair_row_bytes(const Request &R)
 {
     const int64_t K = 4 * (int64_t)R.nN;
-    return 16 * (size_t)K * 8 + 2 * (size_t)R.n_slices * 16 * round_up(K, kBK) + 64;
+    return 16 * (size_t)K * 8 + 2 * (size_t)R.n_slices * 16 * round_up(K, kBK) + 3 * 8 + 16 * 4 +
+           64;
 }
 
 int split_pair_prepare(Engine *E, const Request &R, cudaStream_t st, const double *f2,
@@ -1252,6 +1293,10 @@ int split_pair_prepare(Engine *E, const Request &R, cudaStream_t st, const doubl
     sp.Fd = (double *)p;
     CUTC_TRY(W.get(slot0 + SS_C64, (size_t)16 * n1t * K * 8, &p));
     sp.Cd = (double *)p;
+    CUTC_TRY(W.get(slot0 + SS_R1D, (size_t)3 * n1t * sizeof(float2), &p));
+    sp.r1d = (float2 *)p;
+    CUTC_TRY(W.get(slot0 + SS_BSCALE, (size_t)round_up(16 * n1t, bn_for(kPairTcSlices)) * 4, &p));
+    sp.bscale = (float *)p;
     CUTC_TRY(alloc_operand(W, slot0 + SS_AF, kPairTcSlices, R.n2, kBM, K, sp.AF));
     CUTC_TRY(alloc_operand(W, slot0 + SS_BC, kPairTcSlices, (int)(16 * n1t),
                            bn_for(kPairTcSlices), K, sp.BC));
@@ -1300,12 +1345,14 @@ int split_pair_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
         return CUTC_OK;
     const int64_t K = 4 * (int64_t)P.nN;
     CUTC_TRY(launch_pair_tc_coef(st, P.i0, P.n1b, P.nN, P.r1, rn, a_en, P.coef, P.exps,
-                                 P.term_off, sp.Cd));
+                                 P.term_off, sp.Cd, sp.r1d));
     Operand B = sp.BC;
     B.M = 16 * P.n1b;
     B.Mpad = (int)round_up(B.M, BN);
     SrcDense src{sp.Cd, K};
     CUTC_TRY((slice_rows<S, SrcDense>(st, src, B)));
+    exp_scale_kernel<<<ceil_div(B.Mpad, 256), 256, 0, st>>>(B.ex, B.Mpad, sp.bscale);
+    CUTC_CUDA_TRY(cudaGetLastError());
     CUtensorMap ta, tb;
     CUTC_TRY(make_tmap(&ta, sp.AF.sl, (int64_t)S * sp.AF.Mpad, sp.AF.Kpad, kBM));
     CUTC_TRY(make_tmap(&tb, B.sl, (int64_t)S * B.Mpad, B.Kpad, BN));
@@ -1316,7 +1363,8 @@ int split_pair_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
     Q.Mpad = sp.AF.Mpad;
     Q.Npad = B.Mpad;
     Q.ea = sp.AF.ex;
-    Q.eb = B.ex;
+    Q.bscale = sp.bscale;
+    Q.r1d = sp.r1d;
     Q.P = P;
     Q.err = sp.err;
     const int KB = (int)(sp.AF.Kpad / kBK);
@@ -1328,7 +1376,7 @@ int split_pair_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
         cutc_set_error(CUTC_ERR_INVALID, "pair contraction of K = %lld", (long long)K);
         return CUTC_ERR_INVALID;
     }
-    note_launches(2);
+    note_launches(3);
     return CUTC_OK;
 }
 

@@ -31,6 +31,8 @@ struct SplitPlan {
     bool pair_tc = false;
     Operand AF, BC;
     double *Fd = nullptr, *Cd = nullptr;
+    float2 *r1d = nullptr;             // the tile's r1 points in double-float
+    float *bscale = nullptr;           // 2^(row exponent) of the coefficient rows
     int2 *pairs_sym = nullptr;         // (a, b), a >= b, in tri_index order
     int2 *pairs_anti = nullptr;        // (a, b), a > b, in stri_index order
     int *err = nullptr;                // device flag set by a bounded wait that gave up

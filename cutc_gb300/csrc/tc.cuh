@@ -236,6 +236,13 @@ __device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b)
     return d;
 }
 
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b)
+{
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 __device__ __forceinline__ float f2_lo(uint64_t a) { return __uint_as_float((uint32_t)a); }
 __device__ __forceinline__ float f2_hi(uint64_t a) { return __uint_as_float((uint32_t)(a >> 32)); }
 
