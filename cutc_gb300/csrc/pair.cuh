@@ -30,6 +30,10 @@ struct PairArgs {
     int64_t plane;
 };
 
+// r12^2 below which the split form's pair kernels take the coordinate differences in
+// FP64 (where they are exact) instead of double-float.
+constexpr float kNearPairR2 = 1.0e-4f;
+
 // Arguments of the double-float pair kernel (split form).
 struct PairDfArgs {
     int i0, n1b, n2, nN;

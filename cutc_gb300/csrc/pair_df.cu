@@ -14,16 +14,16 @@
 //   kernel evaluates both polynomials by Horner's rule in df arithmetic
 //   (~43 df multiply-adds per nucleus for exponents <= 4), then
 //     grad1 u = sum_A du/df1A grad f1A + du/dg grad g12.
-//   * Pairs closer than 0.01 bohr (e-e coalescence) are evaluated entirely in
-//     FP64 with the reference's own term-by-term formula and its r^2 > 1e-15
-//     guard; e-n coalescence is handled by the FP64 per-point terms.
+//   * For pairs closer than 0.01 bohr (e-e coalescence) the coordinate
+//     differences are taken in FP64, where they are exact, and the reference's
+//     r^2 > 1e-15 guard applies; e-n coalescence is handled by the FP64
+//     per-point terms.
 //   * Output is G[c][i][j] as (hi, lo) float pairs; hi + lo is exact in FP64.
 #include <algorithm>
 
 #include "common.cuh"
 #include "dfloat.cuh"
 #include "pair.cuh"
-#include "pair_near.cuh"
 
 namespace cutc {
 
@@ -152,27 +152,40 @@ pair_df_kernel(PairDfArgs P)
 
     for (int r = 0; r < nrows; r++) {
         const float2 *rr = s_r1 + 3 * r;
-        const df::D dx = df::sub(df::make(rr[0].x, rr[0].y), df::make(x2.x, x2.y));
-        const df::D dy = df::sub(df::make(rr[1].x, rr[1].y), df::make(y2.x, y2.y));
-        const df::D dz = df::sub(df::make(rr[2].x, rr[2].y), df::make(z2.x, z2.y));
-        const df::D d2 = df::add(df::add(df::sqr(dx), df::sqr(dy)), df::sqr(dz));
+        df::D dx = df::sub(df::make(rr[0].x, rr[0].y), df::make(x2.x, x2.y));
+        df::D dy = df::sub(df::make(rr[1].x, rr[1].y), df::make(y2.x, y2.y));
+        df::D dz = df::sub(df::make(rr[2].x, rr[2].y), df::make(z2.x, z2.y));
+        df::D d2 = df::add(df::add(df::sqr(dx), df::sqr(dy)), df::sqr(dz));
         const int64_t o = (int64_t)(row0 + r) * P.ldg + j;
         float2 w4[4];
+        bool coalesced = false;
         if (d2.hi < kNearPairR2) {
-            double v[4];
-            pair_fp64_single(P, row0 + r, j, v);
-            for (int c = 0; c < 4; c++) {
-                const df::D w = df::from_double(v[c]);
-                w4[c] = make_float2(w.hi, w.lo);
-            }
-        } else {
+            // near e-e coalescence the differences are taken in FP64, where they are exact
+            // (the coordinates' double-float forms keep only 48 bits); only g12 and its
+            // gradient depend on them.  The reference's guard, r12^2 <= 1e-15
+            // (src/jast_bh.cu:143), gives g = 0.
+            const double *a1 = P.r1 + 3 * (int64_t)(P.i0 + row0 + r);
+            const double *a2 = P.r2 + 3 * (int64_t)j;
+            const double ex = a1[0] - a2[0], ey = a1[1] - a2[1], ez = a1[2] - a2[2];
+            dx = df::from_double(ex);
+            dy = df::from_double(ey);
+            dz = df::from_double(ez);
+            d2 = df::add(df::add(df::sqr(dx), df::sqr(dy)), df::sqr(dz));
+            coalesced = !(ex * ex + ey * ey + ez * ez > 1e-15);
+        }
+        {
             // g = a r / (1 + a r), grad g = a / (r (1 + a r)^2) (r1 - r2)
-            const df::D rd = df::sqrt(d2);
-            const df::D ar = df::mul(rd, a);
-            const df::D t = df::recip(df::add_f(ar, 1.0f));
-            const df::D g = df::mul(ar, t);
-            const df::D s = df::mul(df::mul(df::sqr(t), a), df::recip(rd));
-            const df::D gx = df::mul(s, dx), gy = df::mul(s, dy), gz = df::mul(s, dz);
+            df::D g = {0.f, 0.f}, gx = {0.f, 0.f}, gy = {0.f, 0.f}, gz = {0.f, 0.f};
+            if (!coalesced) {
+                const df::D rd = df::sqrt(d2);
+                const df::D ar = df::mul(rd, a);
+                const df::D t = df::recip(df::add_f(ar, 1.0f));
+                g = df::mul(ar, t);
+                const df::D s = df::mul(df::mul(df::sqr(t), a), df::recip(rd));
+                gx = df::mul(s, dx);
+                gy = df::mul(s, dy);
+                gz = df::mul(s, dz);
+            }
 
             df::D ux = {0.f, 0.f}, uy = {0.f, 0.f}, uz = {0.f, 0.f}, dudg = {0.f, 0.f};
             const float2 *cr = s_coef + r * per_row;

@@ -51,7 +51,6 @@
 #include "dfloat.cuh"
 #include "digits.cuh"
 #include "pair.cuh"
-#include "pair_near.cuh"
 #include "products.cuh"
 #include "split.cuh"
 #include "tc.cuh"
