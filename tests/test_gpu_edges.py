@@ -63,3 +63,26 @@ def test_split_tile_with_more_than_65535_g_rows():
     assert st["n_r1_tiles"] == 1
     Xo, Io = oracle.cutc_int(p)
     _check(X, I, Xo, Io, cg.SPLIT_BF16)
+
+
+def test_split_x_with_more_than_65535_packed_pairs():
+    """n_ao = 370: 68 635 packed AO pairs, so the X contraction's A operand has more rows
+    than a grid dimension holds (the slicer takes rows grid-stride).  X alone (int_2e
+    would be 150 GB), against the oracle's windowed X."""
+    import torch
+    p = synth.make_problem(n_nuc=2, n_ao=370, n_grid1=24, n_grid2=400, size_bh=4, seed=42)
+    nA2 = p.n_ao ** 2
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in p.arrays().items()}
+    X = torch.empty((3, p.n_grid1, nA2), dtype=torch.float64, device="cuda")
+    opt = cg.options(cg.SPLIT_BF16, None, p.a_en, p.a_ee, 3, True)
+    s = cg.cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh, d["r1"], d["wr1"],
+                       d["r2"], d["wr2"], d["rn"], d["aos1"], d["aos2"], d["c_bh"], d["m_bh"],
+                       d["n_bh"], d["o_bh"], X, None)
+    torch.cuda.synchronize()
+    assert s == cg.CUTC_OK, cg.last_error()
+    Xo = oracle.x_rows(p)[:3]
+    e = oracle.rel_err(X.cpu().numpy(), Xo)
+    assert e["norm"] < TOL[cg.SPLIT_BF16] and e["max"] < TOL[cg.SPLIT_BF16], e
+    del X, d
+    torch.cuda.empty_cache()
+    cg.load().cutc_release()
