@@ -35,7 +35,7 @@ EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_int_scan", "cutc_default_options", "
            "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
            "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy",
            "trans_inplace", "trans_pqst_psqt_inplace", "trans_pqst_psqt_copy", "cutc_eval_aos",
-           "cutc_x_ao_to_mo", "cutc_plan", "cutc_pin_host", "cutc_unpin_host",
+           "cutc_x_ao_to_mo", "cutc_no_2e", "cutc_plan", "cutc_pin_host", "cutc_unpin_host",
            "cutc_int_bh", "int_long_range", "int_short_range_herm", "int_short_range_nonherm",
            "get_int2_grad1_u12_ao", "get_int_2e_ao"]
 
@@ -162,6 +162,8 @@ def load(path: str = LIB_PATH):
     L.cutc_fp64_gemm_dev.argtypes = [i, i, i, ll, ctypes.c_double, vp, ll, ll, vp, ll, ll,
                                      ctypes.c_double, vp, ll, ll, i]
     L.cutc_fp64_gemm_dev.restype = i
+    L.cutc_no_2e.argtypes = [ctypes.POINTER(Options), i, i, vp, vp, vp, vp, vp]
+    L.cutc_no_2e.restype = i
     L.cutc_validate_launch_dims.argtypes = [i] * 6
     L.cutc_validate_launch_dims.restype = i
     L.cutc_last_error.argtypes = []
@@ -449,6 +451,27 @@ def jast_bh_device_noalloc(r1, r2, rn, c_bh, m_bh, n_bh, o_bh, G, i0=0, n1b=None
     return L.cutc_jast_bh_dev_noalloc(i0, n1b, n1, r2.shape[0], rn.shape[0], c_bh.shape[1],
                                       _vp(r1), _vp(r2), _vp(rn), _vp(c_bh), _vp(m_bh), _vp(n_bh),
                                       _vp(o_bh), a_en, a_ee, _vp(G), stream)
+
+
+def no_2e(tmpC1, x_mo, tmpC2, tmpD2, n_mo, n_grid1, precision=PLAIN_FP64, n_slices=None,
+          out=None):
+    """The two-electron contraction of cutc_no on its intermediates (cutc_no_2e): numpy
+    arrays (host) or torch tensors (device), FP64, in the reference's layouts; returns
+    no_2e (n_mo^4, as an (n_mo^2, n_mo^2) array of Fortran order)."""
+    dev = hasattr(tmpC1, "data_ptr")
+    if out is None:
+        if dev:
+            import torch
+            out = torch.empty((n_mo * n_mo, n_mo * n_mo), dtype=torch.float64,
+                              device=tmpC1.device)
+        else:
+            out = np.empty((n_mo * n_mo, n_mo * n_mo))
+    opt = options(precision, n_slices, device_pointers=dev)
+    s = load().cutc_no_2e(ctypes.byref(opt), n_mo, n_grid1, _vp(tmpC1), _vp(x_mo), _vp(tmpC2),
+                          _vp(tmpD2), _vp(out))
+    if s != CUTC_OK:
+        raise CutcError(s, last_error())
+    return out
 
 
 def fp64_gemm_device(a_kmajor, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, stride_a=0,

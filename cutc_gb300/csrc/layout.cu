@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "products.cuh"
 
 namespace cutc {
 
@@ -84,6 +85,35 @@ static void record(const char *what)
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         cutc_set_error(CUTC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int launch_add_transpose(cudaStream_t st, double *a, int n)
+{
+    const unsigned nb = ceil_div(n, 32);
+    if (n <= 0)
+        return CUTC_OK;
+    if (nb > 65535u) {
+        cutc_set_error(CUTC_ERR_INVALID, "A + A^T of order %d: too large", n);
+        return CUTC_ERR_INVALID;
+    }
+    add_transpose_kernel<<<dim3(nb, nb), dim3(32, 8), 0, st>>>(a, n);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    note_launches(1);
+    return CUTC_OK;
+}
+
+int launch_swap_qs(cudaStream_t st, double *d, int n)
+{
+    if (n <= 0)
+        return CUTC_OK;
+    if (n > 65535) {
+        cutc_set_error(CUTC_ERR_INVALID, "(q, s) swap of order %d: too large", n);
+        return CUTC_ERR_INVALID;
+    }
+    swap_qs_kernel<<<dim3(n, n), 128, 0, st>>>(d, n);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    note_launches(1);
+    return CUTC_OK;
 }
 
 }  // namespace cutc

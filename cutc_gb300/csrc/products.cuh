@@ -21,5 +21,9 @@ int launch_expand_pairs(cudaStream_t st, int64_t rows, int nA, const double *Xp,
 // psqt: element (p,q,s,t) goes where (p,s,q,t) would (c0 and c1 multiples of nA).
 int launch_assemble_int2e(cudaStream_t st, int nA, const double *H, const double *N, int c0,
                           int c1, bool psqt, double *out);
+// a <- a + a^T (column-major n x n), and the (p,q,s,t) -> (p,s,q,t) swap of an n^4 array,
+// on a stream (layout.cu; the reference-named helpers use the legacy default stream)
+int launch_add_transpose(cudaStream_t st, double *a, int n);
+int launch_swap_qs(cudaStream_t st, double *d, int n);
 
 }  // namespace cutc

@@ -743,6 +743,16 @@ struct SrcDense {  // X[r * ld + k]
     __device__ double operator()(int64_t r, int64_t k) const { return X[r * ld + k]; }
 };
 
+struct SrcConcat {  // [X1 | X2]: X1[r * k1 + k] for k < k1, then X2[r * k2 + k - k1]
+    static constexpr bool kDoubleFloat = false;
+    const double *X1, *X2;
+    int64_t k1, k2;
+    __device__ double operator()(int64_t r, int64_t k) const
+    {
+        return k < k1 ? X1[r * k1 + k] : X2[r * k2 + (k - k1)];
+    }
+};
+
 struct SrcDenseDF {  // hi + lo of X[r * ld + k]; the slicer reads the pair itself
     static constexpr bool kDoubleFloat = true;
     const float2 *X;
@@ -1409,6 +1419,40 @@ int split_gemm_dense(Engine *E, cudaStream_t st, int n_slices, int M, int N, int
         CUTC_TRY((slice_rows<S, SrcDense>(st, sa, OA)));
         CUTC_TRY((slice_rows<S, SrcDense>(st, sb, OB)));
         CUTC_TRY(gemm<S>(st, OA, OB, 1.0, C, ldc, N, 0, 0, 0, err));
+    });
+    int herr = 0;
+    CUTC_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+    CUTC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (herr) {
+        cutc_set_error(CUTC_ERR_TIMEOUT, "a tensor-core pipeline wait gave up (code %d)", herr);
+        return CUTC_ERR_TIMEOUT;
+    }
+    return CUTC_OK;
+}
+
+// C[m + ldc n] = alpha sum_k [A1 | A2][m, k] [B1 | B2][n, k] through the split form: the
+// two products of the same output as ONE contraction over K1 + K2 (one row scale per row
+// of the concatenation, exact accumulation over all of it).  A1, B1 are K1-contiguous,
+// A2, B2 K2-contiguous (device arrays); synchronous on st.
+int split_gemm_concat(Engine *E, cudaStream_t st, int n_slices, int M, int N, int64_t K1,
+                      const double *A1, const double *B1, int64_t K2, const double *A2,
+                      const double *B2, double alpha, double *C, int64_t ldc)
+{
+    Workspace &W = E->ws;
+    const int base = 210;
+    const int64_t K = K1 + K2;
+    Operand OA, OB;
+    CUTC_TRY(alloc_operand(W, base, n_slices, M, kBM, K, OA));
+    CUTC_TRY(alloc_operand(W, base + 3, n_slices, N, bn_for(n_slices), K, OB));
+    void *p;
+    CUTC_TRY(W.get(base + 6, 64, &p));
+    int *err = (int *)p;
+    CUTC_CUDA_TRY(cudaMemsetAsync(err, 0, 4, st));
+    SrcConcat sa{A1, A2, K1, K2}, sb{B1, B2, K1, K2};
+    CUTC_SLICES_DISPATCH(n_slices, {
+        CUTC_TRY((slice_rows<S, SrcConcat>(st, sa, OA)));
+        CUTC_TRY((slice_rows<S, SrcConcat>(st, sb, OB)));
+        CUTC_TRY(gemm<S>(st, OA, OB, alpha, C, ldc, N, 0, 0, 0, err));
     });
     int herr = 0;
     CUTC_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));

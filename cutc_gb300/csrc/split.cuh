@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include "engine.cuh"
+#include "pair.cuh"
 
 namespace cutc {
 
@@ -83,5 +84,10 @@ int split_check(cudaStream_t st, SplitPlan &sp);
 // C[m + ldc n] = sum_k A[m K + k] B[n K + k] through the split form (device arrays)
 int split_gemm_dense(Engine *E, cudaStream_t st, int n_slices, int M, int N, int64_t K,
                      const double *A, const double *B, double *C, int64_t ldc);
+// C[m + ldc n] = alpha (A1[m K1 + k] B1[n K1 + k] summed over k < K1 + A2 B2^T likewise
+// over K2), as one split contraction over the concatenated K (device arrays)
+int split_gemm_concat(Engine *E, cudaStream_t st, int n_slices, int M, int N, int64_t K1,
+                      const double *A1, const double *B1, int64_t K2, const double *A2,
+                      const double *B2, double alpha, double *C, int64_t ldc);
 
 }  // namespace cutc

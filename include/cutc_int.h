@@ -331,6 +331,20 @@ int cutc_x_ao_to_mo(int n_grid1, int n_ao, int n_mo, int components,
                     const double *mo_l_coef, const double *mo_r_coef,
                     const double *x_ao, double *x_mo, int device_pointers, void *stream);
 
+/*
+ * The two-electron contraction of the reference's cutc_no (src/cutc_no.c:415-470), on its
+ * intermediates: with M = n_mo^2 MO pairs,
+ *   no_2e = 1/2 tmpC1^T x_mo + 1/2 tmpC2^T tmpD2,  then no_2e <- no_2e + no_2e^T,
+ *   then the (p,q,s,t) -> (p,s,q,t) swap of trans_pqst_psqt_inplace.
+ * x_mo is X in the MO basis in cutc_no's order, [(g + n_grid1 m) + 3 n_grid1 (i + n_mo j)]
+ * (what cutc_x_ao_to_mo writes); tmpC1 has the same layout (3 n_grid1 x n_mo^2), tmpC2 and
+ * tmpD2 are n_grid1 x n_mo^2, no_2e is n_mo^4 (all column-major, FP64).  Options used:
+ * precision (plain FP64 as the reference, or the split form: one split contraction over
+ * the concatenated K = 4 n_grid1), n_slices, device_pointers, stream.  Synchronous.
+ */
+int cutc_no_2e(const cutc_options *opt, int n_mo, int n_grid1, const double *tmpC1,
+               const double *x_mo, const double *tmpC2, const double *tmpD2, double *no_2e);
+
 /* ---- reference helpers with the reference's names and semantics ------------
  * Device pointers; launched on the legacy default stream without a host
  * synchronisation, as the reference does; errors are recorded for
