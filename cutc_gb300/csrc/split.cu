@@ -43,6 +43,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdlib>
 #include <vector>
@@ -86,7 +87,8 @@ struct GemmParams {
     int kb0, nkb;          // K blocks [kb0, kb0 + nkb) of this launch
     const int *ea;         // row exponents of A (Mpad)
     const int *eb;         // row exponents of B (Npad)
-    double alpha;
+    double alpha;          // result x 2^alpha_exp, negated if alpha_neg, x alpha if alpha_mul
+    int alpha_exp, alpha_neg, alpha_mul;
     double *C;
     int64_t ldc;           // C[m + ldc * col(n)]
     int ncol_group;        // col(n) = (n / ncol_group) * group_stride + col0 + n % ncol_group
@@ -122,6 +124,17 @@ __device__ __forceinline__ double pow2(int e)
 {
     e = e < -1022 ? -1022 : (e > 1023 ? 1023 : e);
     return __longlong_as_double((long long)(1023 + e) << 52);
+}
+
+// v 2^k exactly: the exponent field moved with integer operations when the result stays
+// a normal number (GB300's FP64 pipe is slow), a multiplication otherwise
+__device__ __forceinline__ double scale_pow2(double v, int k)
+{
+    const long long b = __double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e != 0 && e + k >= 1 && e + k <= 2046)
+        return __longlong_as_double(b + ((long long)k << 52));
+    return e == 0 && (b << 1) == 0 ? v : v * pow2(k);
 }
 
 template <int S>
@@ -330,16 +343,38 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const int m = m0 + q * 32 + lane;
         if (ok && m < P.M) {
             const int em = P.ea[m];
+            // The seven exact FP32 parts of each column, two columns per f32x2 operation:
+            // hi0 + hi1 + lo0 + hi2 + lo1 by TwoSum (exact), the rounding errors and the
+            // small lo2 and s3 in FP32 (below 2^-46 of the total), then one conversion to
+            // FP64 per part and one FP64 add.  The power-of-two scale goes into the
+            // exponent bits: GB300's FP64 pipe is slow, so the epilogue keeps off it.
+            auto two_sum = [](uint64_t a, uint64_t b, uint64_t &e) -> uint64_t {
+                const uint64_t sm = tc::f2_add(a, b);
+                const uint64_t bb = tc::f2_sub(sm, a);
+                e = tc::f2_add(tc::f2_sub(a, tc::f2_sub(sm, bb)), tc::f2_sub(b, bb));
+                return sm;
+            };
 #pragma unroll
-            for (int j = 0; j < CW; j++) {
-                const int n = n0 + (int)coff + j;
-                if (n < P.N) {
-                    auto lane_of = [&](const uint64_t (&a)[CP]) -> double {
-                        return (double)((j & 1) ? tc::f2_hi(a[j >> 1]) : tc::f2_lo(a[j >> 1]));
-                    };
-                    double val = ((lane_of(hi0) + lane_of(hi1)) + (lane_of(hi2) + lane_of(lo0))) +
-                                 ((lane_of(lo1) + lane_of(lo2)) + lane_of(s3));
-                    val *= P.alpha * pow2(em + P.eb[n]);
+            for (int k = 0; k < CP; k++) {
+                uint64_t e1, e2, e3, e4;
+                uint64_t sm = two_sum(hi0[k], hi1[k], e1);
+                sm = two_sum(sm, lo0[k], e2);
+                sm = two_sum(sm, hi2[k], e3);
+                sm = two_sum(sm, lo1[k], e4);
+                const uint64_t lo = tc::f2_add(tc::f2_add(tc::f2_add(e1, e2), tc::f2_add(e3, e4)),
+                                               tc::f2_add(lo2[k], s3[k]));
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int n = n0 + (int)coff + 2 * k + h;
+                    if (n >= P.N)
+                        continue;
+                    const float sh = h ? tc::f2_hi(sm) : tc::f2_lo(sm);
+                    const float sl = h ? tc::f2_hi(lo) : tc::f2_lo(lo);
+                    double val = scale_pow2((double)sh + (double)sl, em + P.eb[n] + P.alpha_exp);
+                    if (P.alpha_neg)
+                        val = __longlong_as_double(__double_as_longlong(val) ^ (1ll << 63));
+                    if (P.alpha_mul)
+                        val *= P.alpha;
                     const int64_t col = (int64_t)(n / P.ncol_group) * P.group_stride + P.col0 +
                                         n % P.ncol_group;
                     double *dst = P.C + m + P.ldc * col;
@@ -1099,6 +1134,12 @@ static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alph
         P.nkb = std::min(kb_per, nkb_total - kb0);
         P.ea = A.ex;
         P.eb = B.ex;
+        // a power of two (1, -1/2, 1/2 in this library) scales through the exponent
+        int ae = 0;
+        const double am = std::frexp(std::fabs(alpha), &ae);
+        P.alpha_mul = am != 0.5;
+        P.alpha_exp = P.alpha_mul ? 0 : ae - 1;
+        P.alpha_neg = !P.alpha_mul && alpha < 0;
         P.alpha = alpha;
         P.C = C;
         P.ldc = ldc;
