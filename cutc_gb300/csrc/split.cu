@@ -33,9 +33,13 @@
 //     rounding would otherwise grow with K;
 //   * the accumulators are double-buffered in tensor memory, so the flush of
 //     chunk c overlaps the MMAs of chunk c + 1;
-//   * at the end the pieces are summed in FP64 and scaled by alpha 2^{e_r + f_n}.
-// FP64 arithmetic is used only in that final recombination (and in the pair
-// terms that feed G), which is where GB300's scarce FP64 rate is affordable.
+//   * at the end the seven FP32 pieces are summed error-free (TwoSum on f32x2 pairs
+//     of columns, the small remainders in FP32), the double-float result is
+//     converted with one FP64 add, and the scale 2^{e_r + f_n} (and a power-of-two
+//     alpha) is added to the exponent bits.
+// FP64 arithmetic is used only in that conversion (and in the pair terms that feed
+// G): GB300's FP64 pipe runs at 1/64 of the FP32 rate, and a full FP64 sum of the
+// pieces cost 7 % of the contraction.
 // The scheme is the error-free splitting of Ozaki, Ogita, Oishi & Rump
 // (2012), on BF16 instead of FP64 slices, with exact FP32 chunk accumulation.
 #include <cuda.h>
