@@ -130,15 +130,16 @@ __device__ __forceinline__ double pow2(int e)
     return __longlong_as_double((long long)(1023 + e) << 52);
 }
 
-// v 2^k exactly: the exponent field moved with integer operations when the result stays
-// a normal number (GB300's FP64 pipe is slow), a multiplication otherwise
+// v 2^k: the exponent field moved with integer operations when v and the result are
+// normal numbers (GB300's FP64 pipe is slow), scalbn otherwise (zeros, and results that
+// underflow to subnormals or zero or overflow to infinity)
 __device__ __forceinline__ double scale_pow2(double v, int k)
 {
     const long long b = __double_as_longlong(v);
     const int e = (int)((b >> 52) & 0x7ff);
     if (e != 0 && e + k >= 1 && e + k <= 2046)
         return __longlong_as_double(b + ((long long)k << 52));
-    return e == 0 && (b << 1) == 0 ? v : v * pow2(k);
+    return scalbn(v, k);
 }
 
 template <int S>
@@ -403,9 +404,14 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 //   V_c(r1, r2) = sum_k C[(r1, c)][k] F[r2][k],  k = 4 A + q over (nucleus, power of f2)
 // (pair_df.cu builds F and the 16 coefficient rows C per r1 point in FP64).  Here it
 // runs as a split contraction: A = the F slices (one 128-row tile of r2 points, all
-// of K, loaded once per CTA), B = the coefficient slices (N tiles of BN rows = BN/16
-// r1 points, streamed), one stacked-diagonal accumulator set per N tile in tensor
-// memory, double-buffered.  K = 4 n_nuc <= 80, so every diagonal sum is one chunk:
+// of K, loaded once per CTA), B = the coefficient slices (N tiles of 64 rows = four
+// r1 points, streamed), one stacked-diagonal accumulator set in tensor memory.  The
+// tensor-core work of a tile is about 1/40 of its epilogue, so one accumulator set and
+// one B stage suffice: the next tile's MMAs run as soon as the epilogue has read the
+// accumulators, long before it needs them, and one control warp issues both the TMA
+// loads and the MMAs, which leaves registers for 16 epilogue warps (4 per SM
+// sub-partition) to hide the latency of their dependent double-float chains.
+// K = 4 n_nuc <= 80, so every diagonal sum is one chunk:
 // diagonals 0..2 are exact in FP32 ((d + 1) * 80 * 2^16 < 2^24), d >= 3 are 2^-27 and
 // below, where FP32 rounding is immaterial.
 //
@@ -438,25 +444,26 @@ __global__ void exp_scale_kernel(const int *__restrict__ ex, int rows, float *__
     }
 }
 
+constexpr int kPairBN = 64;  // coefficient rows per N tile: four r1 points x 16 columns
+
 template <int S, int KB>
 struct PairTcCfg {
-    static constexpr int kBN = bn_for(S);            // 48: three r1 points per N tile
+    static constexpr int kBN = kPairBN;
     static constexpr int kPts = kBN / 16;
     static constexpr int kEpiWarps = 4 * kPts;       // lane quarter x r1 point
-    static constexpr int kTmaWarp = kEpiWarps;
-    static constexpr int kMmaWarp = kEpiWarps + 1;
-    static constexpr int kThreads = (kEpiWarps + 2) * 32;
+    static constexpr int kCtlWarp = kEpiWarps;       // TMA loads and MMAs, lane 0
+    static constexpr int kThreads = (kEpiWarps + 1) * 32;
     static constexpr int kASlice = kBM * kBK * 2;
     static constexpr int kBSlice = kBN * kBK * 2;
     static constexpr int kABytes = KB * S * kASlice;
-    static constexpr int kStages = 2;
     static constexpr int kBStage = KB * S * kBSlice;
-    static constexpr int kBuf = kBN * S;             // tensor-memory columns per buffer
-    static constexpr int kSmem = kABytes + kStages * kBStage + 1024 + 256;
+    static constexpr int kSmem = kABytes + kBStage + 1024 + 256;
+    static constexpr int kMaxN = 256;                // widest kind::f16 instruction at M = 128
     static_assert(kSmem <= 227 * 1024, "shared memory");
-    static_assert(2 * kBuf <= (int)kTmemCols, "accumulators exceed tensor memory");
-    static_assert(kBN * S <= 256, "instruction N exceeds 256");
+    static_assert(kBN * S <= (int)kTmemCols, "accumulators exceed tensor memory");
+    static_assert(kMaxN % kBN == 0, "instruction splits on diagonal boundaries");
     static_assert(kBSlice % 512 == 0, "B slices must stack on 8-row swizzle atoms");
+    static_assert(kThreads * 120 <= 65536, "registers for one CTA per SM");
 };
 
 // x 2^e for the scale of a value of row exponents e (clamped to the float range)
@@ -473,20 +480,19 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 {
     using Cfg = PairTcCfg<S, KB>;
     constexpr int D = S - 1, BN = Cfg::kBN;
-    constexpr int kEpiWarps = Cfg::kEpiWarps, kTmaWarp = Cfg::kTmaWarp, kMmaWarp = Cfg::kMmaWarp;
-    constexpr int kStages = Cfg::kStages;
+    constexpr int kEpiWarps = Cfg::kEpiWarps, kCtlWarp = Cfg::kCtlWarp;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
     uint8_t *sB = smem + Cfg::kABytes;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + kStages * Cfg::kBStage);
-    uint64_t *afull = bars;
-    uint64_t *full = bars + 1;
-    uint64_t *empty = full + kStages;
-    uint64_t *tfull = empty + kStages;
-    uint64_t *tempty = tfull + 2;
-    uint64_t *drain = tempty + 2;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + Cfg::kBStage);
+    uint64_t *afull = bars;      // the F tile has landed
+    uint64_t *full = bars + 1;   // the B stage holds tile q
+    uint64_t *empty = bars + 2;  // the MMAs of tile q are done with the B stage
+    uint64_t *tfull = bars + 3;  // the accumulators hold tile q
+    uint64_t *tempty = bars + 4; // every epilogue warp has read tile q's accumulators
+    uint64_t *drain = bars + 5;
     uint32_t *s_tmem = reinterpret_cast<uint32_t *>(drain + 1);
     volatile int *s_abort = reinterpret_cast<volatile int *>(s_tmem + 1);
 
@@ -497,26 +503,19 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     const int ntiles = min(Q.tiles_n, t_begin + Q.chunk) - t_begin;
 
     if (threadIdx.x == 0) {
-        tc::mbar_init(tc::smem_u32(afull), 1);
-        for (int i = 0; i < kStages; i++) {
-            tc::mbar_init(tc::smem_u32(&full[i]), 1);
-            tc::mbar_init(tc::smem_u32(&empty[i]), 1);
-        }
-        for (int i = 0; i < 2; i++) {
-            tc::mbar_init(tc::smem_u32(&tfull[i]), 1);
-            tc::mbar_init(tc::smem_u32(&tempty[i]), kEpiWarps);
-        }
+        for (int i = 0; i < 5; i++)
+            tc::mbar_init(tc::smem_u32(&bars[i]), i == 4 ? kEpiWarps : 1);
         tc::mbar_init(tc::smem_u32(drain), 1);
         *s_abort = 0;
         tc::fence_mbar_init();
     }
-    if (warp == kMmaWarp) {
+    if (warp == kCtlWarp) {
         tc::tmem_alloc(tc::smem_u32(s_tmem), kTmemCols);
         tc::tmem_relinquish();
-    }
-    if (warp == kTmaWarp && lane == 0) {
-        tc::tma_prefetch(&tmA);
-        tc::tma_prefetch(&tmB);
+        if (lane == 0) {
+            tc::tma_prefetch(&tmA);
+            tc::tma_prefetch(&tmB);
+        }
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -528,8 +527,19 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         atomicExch(Q.err, code);
     };
 
-    if (warp == kTmaWarp) {
+    if (warp == kCtlWarp) {
         if (lane == 0) {
+            auto load_b = [&](int q) {
+                const uint32_t fb = tc::smem_u32(full);
+                tc::mbar_arrive_expect_tx(fb, Cfg::kBStage);
+                const int n0 = (t_begin + q) * BN;
+#pragma unroll
+                for (int kb = 0; kb < KB; kb++)
+#pragma unroll
+                    for (int t = 0; t < S; t++)
+                        tc::tma_load_2d(tc::smem_u32(sB + (kb * S + t) * Cfg::kBSlice), &tmB,
+                                        kb * kBK, t * Q.Npad + n0, fb);
+            };
             const uint32_t ab = tc::smem_u32(afull);
             tc::mbar_arrive_expect_tx(ab, Cfg::kABytes);
 #pragma unroll
@@ -538,76 +548,69 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 for (int s = 0; s < S; s++)
                     tc::tma_load_2d(tc::smem_u32(sA + (kb * S + s) * Cfg::kASlice), &tmA, kb * kBK,
                                     s * Q.Mpad + m0, ab);
-            int issued = 0;
-            for (int q = 0; q < ntiles; q++) {
-                const int stage = q % kStages, round = q / kStages;
-                if (round > 0 &&
-                    !tc::mbar_wait(tc::smem_u32(&empty[stage]), (round - 1) & 1, s_abort)) {
-                    fail(11);
-                    break;
-                }
-                const uint32_t fb = tc::smem_u32(&full[stage]);
-                tc::mbar_arrive_expect_tx(fb, Cfg::kBStage);
-                uint8_t *st = sB + stage * Cfg::kBStage;
-                const int n0 = (t_begin + q) * BN;
-#pragma unroll
-                for (int kb = 0; kb < KB; kb++)
-#pragma unroll
-                    for (int t = 0; t < S; t++)
-                        tc::tma_load_2d(tc::smem_u32(st + (kb * S + t) * Cfg::kBSlice), &tmB,
-                                        kb * kBK, t * Q.Npad + n0, fb);
-                issued = q + 1;
+            int loaded = 0;  // B tiles issued into the stage
+            if (ntiles > 0) {
+                load_b(0);
+                loaded = 1;
             }
-            // let the copies still in flight land before the CTA goes away
-            tc::mbar_wait(ab, 0, nullptr);
-            if (*s_abort) {
-                for (int q = max(0, issued - kStages); q < issued; q++)
-                    tc::mbar_wait(tc::smem_u32(&full[q % kStages]), (q / kStages) & 1, nullptr);
-            }
-        }
-    } else if (warp == kMmaWarp) {
-        if (lane == 0) {
-            bool ok = tc::mbar_wait(tc::smem_u32(afull), 0, s_abort);
+            bool ok = tc::mbar_wait(ab, 0, s_abort);
             if (!ok)
                 fail(12);
             for (int q = 0; q < ntiles && ok; q++) {
-                const int b = q & 1, stage = q % kStages;
-                if (q >= 2 && !tc::mbar_wait(tc::smem_u32(&tempty[b]), ((q >> 1) - 1) & 1, s_abort)) {
+                // the accumulators are free once every epilogue warp has read tile q - 1
+                if (q >= 1 && !tc::mbar_wait(tc::smem_u32(tempty), (q - 1) & 1, s_abort)) {
                     fail(13);
                     break;
                 }
-                if (!tc::mbar_wait(tc::smem_u32(&full[stage]), (q / kStages) & 1, s_abort)) {
+                if (!tc::mbar_wait(tc::smem_u32(full), q & 1, s_abort)) {
                     fail(14);
                     break;
                 }
                 tc::fence_after_sync();
-                const uint32_t sb0 = tc::smem_u32(sB + stage * Cfg::kBStage);
+                const uint32_t sb0 = tc::smem_u32(sB);
                 const uint32_t sa0 = tc::smem_u32(sA);
                 bool first = true;
 #pragma unroll
                 for (int kb = 0; kb < KB; kb++) {
 #pragma unroll
                     for (int k16 = 0; k16 < kBK / 16; k16++) {
-                        const uint64_t bd =
-                            tc::smem_desc_sw64(sb0 + kb * S * Cfg::kBSlice + k16 * 32);
 #pragma unroll
                         for (int s = 0; s < S; s++) {
-                            // a_s x [b_0 .. b_{D-s}] -> diagonals s .. D
-                            const uint32_t idesc = tc::idesc_bf16_f32(kBM, BN * (D + 1 - s));
+                            // a_s x [b_0 .. b_{D-s}] -> diagonals s .. D, in instructions of
+                            // at most kMaxN columns
                             const uint64_t ad = tc::smem_desc_sw64(
                                 sa0 + (kb * S + s) * Cfg::kASlice + k16 * 32);
-                            tc::mma_bf16(tbase + (uint32_t)(Cfg::kBuf * b + BN * s), ad, bd,
-                                         idesc, first ? 0u : 1u);
+#pragma unroll
+                            for (int t0 = 0; t0 <= D - s; t0 += Cfg::kMaxN / BN) {
+                                const int nt = min(Cfg::kMaxN / BN, D - s + 1 - t0);
+                                const uint64_t bd = tc::smem_desc_sw64(
+                                    sb0 + (kb * S + t0) * Cfg::kBSlice + k16 * 32);
+                                tc::mma_bf16(tbase + (uint32_t)(BN * (s + t0)), ad, bd,
+                                             tc::idesc_bf16_f32(kBM, BN * nt), first ? 0u : 1u);
+                            }
                             first = false;
                         }
                     }
                 }
-                tc::mma_commit(tc::smem_u32(&empty[stage]));
-                tc::mma_commit(tc::smem_u32(&tfull[b]));
+                tc::mma_commit(tc::smem_u32(empty));
+                tc::mma_commit(tc::smem_u32(tfull));
+                // refill the B stage for tile q + 1 once these MMAs have read it
+                if (q + 1 < ntiles) {
+                    if (!tc::mbar_wait(tc::smem_u32(empty), q & 1, s_abort)) {
+                        fail(11);
+                        break;
+                    }
+                    load_b(q + 1);
+                    loaded = q + 2;
+                }
             }
             tc::mma_commit(tc::smem_u32(drain));
             if (!tc::mbar_wait(tc::smem_u32(drain), 0, nullptr))
                 fail(15);
+            // let the copies still in flight land before the CTA goes away
+            tc::mbar_wait(ab, 0, nullptr);
+            if (*s_abort && loaded > 0)
+                tc::mbar_wait(tc::smem_u32(full), (loaded - 1) & 1, nullptr);
         }
     } else {
         // ---- epilogue: one r1 point of each N tile, 32 r2 points ---------------------
@@ -620,8 +623,7 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         const float sa = pow2f(Q.ea[jc]);  // F rows: 2^1 (f^0 = 1 is the row maximum)
         const df::D a = df::make(P.a_ee_hi, P.a_ee_lo);
         for (int q = 0; q < ntiles; q++) {
-            const int b = q & 1;
-            if (!tc::mbar_wait(tc::smem_u32(&tfull[b]), (q >> 1) & 1, s_abort)) {
+            if (!tc::mbar_wait(tc::smem_u32(tfull), q & 1, s_abort)) {
                 fail(16);
                 break;
             }
@@ -634,7 +636,7 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             // Two columns share each packed f32x2 operation.
             uint64_t H[8], L[8], L2[8];
             {
-                const uint32_t cb = tbase + lane_off + (uint32_t)(Cfg::kBuf * b + 16 * pt);
+                const uint32_t cb = tbase + lane_off + (uint32_t)(16 * pt);
                 const uint64_t C16 = tc::f2_pack(__float_as_uint(192.0f), __float_as_uint(192.0f));
                 const uint64_t C25 = tc::f2_pack(__float_as_uint(0.375f), __float_as_uint(0.375f));
                 float v[16];
@@ -668,7 +670,7 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             tc::fence_before_sync();
             __syncwarp();
             if (lane == 0)
-                tc::mbar_arrive(tc::smem_u32(&tempty[b]));
+                tc::mbar_arrive(tc::smem_u32(tempty));
 
             const int i = (t_begin + q) * Cfg::kPts + pt;  // r1 row of the tile
             if (i >= P.n1b)
@@ -766,7 +768,7 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (warp == kMmaWarp)
+    if (warp == kCtlWarp)
         tc::tmem_dealloc(tbase, kTmemCols);
 }
 
@@ -1349,11 +1351,11 @@ int split_pair_prepare(Engine *E, const Request &R, cudaStream_t st, const doubl
     sp.Cd = (double *)p;
     CUTC_TRY(W.get(slot0 + SS_R1D, (size_t)3 * n1t * sizeof(float2), &p));
     sp.r1d = (float2 *)p;
-    CUTC_TRY(W.get(slot0 + SS_BSCALE, (size_t)round_up(16 * n1t, bn_for(kPairTcSlices)) * 4, &p));
+    CUTC_TRY(W.get(slot0 + SS_BSCALE, (size_t)round_up(16 * n1t, kPairBN) * 4, &p));
     sp.bscale = (float *)p;
     CUTC_TRY(alloc_operand(W, slot0 + SS_AF, kPairTcSlices, R.n2, kBM, K, sp.AF));
-    CUTC_TRY(alloc_operand(W, slot0 + SS_BC, kPairTcSlices, (int)(16 * n1t),
-                           bn_for(kPairTcSlices), K, sp.BC));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BC, kPairTcSlices, (int)(16 * n1t), kPairBN, K,
+                           sp.BC));
     CUTC_TRY(launch_pair_tc_f(st, R.n2, R.nN, f2, sp.Fd));
     note_launches(1);
     SrcDense src{sp.Fd, K};
@@ -1393,7 +1395,7 @@ int split_pair_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
                     const PairDfArgs &P, const double *rn, double a_en)
 {
     constexpr int S = kPairTcSlices;
-    constexpr int BN = bn_for(S);
+    constexpr int BN = kPairBN;
     (void)R;
     if (P.n1b <= 0 || P.n2 <= 0)
         return CUTC_OK;

@@ -91,3 +91,24 @@ def test_split_gemm_long_k_exact_accumulation():
     C = C.cpu().numpy()
     assert np.all(np.abs(C - R) <= _bound(A, B, 5))
     assert (np.abs(C - R) / Ab).max() < 2.0 ** -40
+
+
+def test_split_gemm_extreme_row_scales():
+    """Row scales 2^-540 .. 2^500 on both sides: products from 2^-1080 (subnormal or zero
+    results) to 2^1000 (near the top of the FP64 range), with the sign of each."""
+    import torch
+    rng = np.random.default_rng(17)
+    M, N, K = 140, 60, 300
+    ea = rng.choice([-540, -300, 0, 300, 500], size=(M, 1))
+    eb = rng.choice([-540, -300, 0, 300, 500], size=(N, 1))
+    A = rng.standard_normal((M, K)) * np.exp2(ea.astype(float))
+    B = rng.standard_normal((N, K)) * np.exp2(eb.astype(float))
+    C = cg.split_gemm_device(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda(), n_slices=5)
+    C = C.cpu().numpy()
+    R, _ = _ref(A, B)
+    assert np.all(np.isfinite(C))
+    # the slice bound, plus K units of the smallest subnormal: numpy's own products round
+    # to subnormals where they underflow
+    assert np.all(np.abs(C - R) <= _bound(A, B, 5) + 2 * K * 2.0 ** -1074)
+    big = (ea + eb.T) >= 0
+    assert np.all(np.sign(C[big]) == np.sign(R[big]))
