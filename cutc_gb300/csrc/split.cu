@@ -1315,27 +1315,31 @@ int split_int2e_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp
 
 // ---- pair terms on the tensor cores -------------------------------------------------
 
-constexpr int kPairTcSlices = 5;   // the slice count the kernel is built for
 constexpr int kPairTcMaxNuc = 20;  // K = 4 n_nuc <= 80 keeps diagonals 0..2 exact
+
+// Slices of the pair contraction's operands: 5 (representation error 2^-45, under the
+// error of a 5-slice build's contractions), or 6 for builds of 6 and 7 slices, whose
+// contractions reach FP64-class errors (2^-54, below the double-float epilogue).
+static int pair_tc_slices(const Request &R) { return R.n_slices >= 6 ? 6 : 5; }
 
 bool split_pair_tc_ok(const Request &R, const int *exps, int n_terms)
 {
-    return R.precision == CUTC_SPLIT_BF16 && !R.pair_fp64 && R.n_slices == kPairTcSlices &&
-           R.nN <= kPairTcMaxNuc && pair_df_sparse(exps, n_terms) && !getenv("CUTC_PAIR_DF") &&
-           !getenv("CUTC_PAIR_DENSE");
+    return R.precision == CUTC_SPLIT_BF16 && !R.pair_fp64 && R.nN <= kPairTcMaxNuc &&
+           pair_df_sparse(exps, n_terms) && !getenv("CUTC_PAIR_DF") && !getenv("CUTC_PAIR_DENSE");
 }
 
 size_t split_pair_fixed_bytes(const Request &R)
 {
     const int64_t K = 4 * (int64_t)R.nN;
-    return (size_t)R.n2 * K * 8 + 2 * (size_t)R.n_slices * round_up(R.n2, kBM) * round_up(K, kBK);
+    return (size_t)R.n2 * K * 8 +
+           2 * (size_t)pair_tc_slices(R) * round_up(R.n2, kBM) * round_up(K, kBK);
 }
 
 size_t split_pair_row_bytes(const Request &R)
 {
     const int64_t K = 4 * (int64_t)R.nN;
-    return 16 * (size_t)K * 8 + 2 * (size_t)R.n_slices * 16 * round_up(K, kBK) + 3 * 8 + 16 * 4 +
-           64;
+    return 16 * (size_t)K * 8 + 2 * (size_t)pair_tc_slices(R) * 16 * round_up(K, kBK) + 3 * 8 +
+           16 * 4 + 64;
 }
 
 int split_pair_prepare(Engine *E, const Request &R, cudaStream_t st, const double *f2,
@@ -1353,13 +1357,17 @@ int split_pair_prepare(Engine *E, const Request &R, cudaStream_t st, const doubl
     sp.r1d = (float2 *)p;
     CUTC_TRY(W.get(slot0 + SS_BSCALE, (size_t)round_up(16 * n1t, kPairBN) * 4, &p));
     sp.bscale = (float *)p;
-    CUTC_TRY(alloc_operand(W, slot0 + SS_AF, kPairTcSlices, R.n2, kBM, K, sp.AF));
-    CUTC_TRY(alloc_operand(W, slot0 + SS_BC, kPairTcSlices, (int)(16 * n1t), kPairBN, K,
-                           sp.BC));
+    const int ps = pair_tc_slices(R);
+    CUTC_TRY(alloc_operand(W, slot0 + SS_AF, ps, R.n2, kBM, K, sp.AF));
+    CUTC_TRY(alloc_operand(W, slot0 + SS_BC, ps, (int)(16 * n1t), kPairBN, K, sp.BC));
     CUTC_TRY(launch_pair_tc_f(st, R.n2, R.nN, f2, sp.Fd));
     note_launches(1);
     SrcDense src{sp.Fd, K};
-    CUTC_TRY((slice_rows<kPairTcSlices, SrcDense>(st, src, sp.AF)));
+    if (ps == 6)
+        CUTC_TRY((slice_rows<6, SrcDense>(st, src, sp.AF)));
+    else
+        CUTC_TRY((slice_rows<5, SrcDense>(st, src, sp.AF)));
+    sp.pair_slices = ps;
     sp.pair_tc = true;
     return CUTC_OK;
 }
@@ -1391,14 +1399,11 @@ static int launch_pair_tc_kernel(cudaStream_t st, const CUtensorMap &ta, const C
     return CUTC_OK;
 }
 
-int split_pair_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
-                    const PairDfArgs &P, const double *rn, double a_en)
+template <int S>
+static int pair_tile(Engine *E, cudaStream_t st, SplitPlan &sp, const PairDfArgs &P,
+                     const double *rn, double a_en)
 {
-    constexpr int S = kPairTcSlices;
     constexpr int BN = kPairBN;
-    (void)R;
-    if (P.n1b <= 0 || P.n2 <= 0)
-        return CUTC_OK;
     const int64_t K = 4 * (int64_t)P.nN;
     CUTC_TRY(launch_pair_tc_coef(st, P.i0, P.n1b, P.nN, P.r1, rn, a_en, P.coef, P.exps,
                                  P.term_off, sp.Cd, sp.r1d));
@@ -1434,6 +1439,16 @@ int split_pair_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
     }
     note_launches(3);
     return CUTC_OK;
+}
+
+int split_pair_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
+                    const PairDfArgs &P, const double *rn, double a_en)
+{
+    (void)R;
+    if (P.n1b <= 0 || P.n2 <= 0)
+        return CUTC_OK;
+    return sp.pair_slices == 6 ? pair_tile<6>(E, st, sp, P, rn, a_en)
+                               : pair_tile<5>(E, st, sp, P, rn, a_en);
 }
 
 int split_check(cudaStream_t st, SplitPlan &sp)

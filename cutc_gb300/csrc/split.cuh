@@ -30,6 +30,7 @@ struct SplitPlan {
     // pair terms on the tensor cores: F slices (powers of f2 on r2), the tile's
     // coefficient slices, and their FP64 sources
     bool pair_tc = false;
+    int pair_slices = 5;
     Operand AF, BC;
     double *Fd = nullptr, *Cd = nullptr;
     float2 *r1d = nullptr;             // the tile's r1 points in double-float

@@ -16,7 +16,9 @@ without forming the n_ao^4 matrix.  The library's outputs stay on the device;
 the test reads X, the same int_2e rows and int_2e v.
 
 Tolerances (relative, normwise and max-abs/max): 1e-12 for the plain FP64
-form (the drop-in), 1e-10 for the split form.
+form (the drop-in), 1e-10 for the split form at its default 5 slices, and
+1e-12 for the split form at 6 slices, which reaches the plain form's error
+class.
 """
 import numpy as np
 import pytest
@@ -28,7 +30,7 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 ROWS = 32
-TOL = {cg.PLAIN_FP64: 1e-12, cg.SPLIT_BF16: 1e-10}
+FORMS = ((cg.SPLIT_BF16, 5, 1e-10), (cg.SPLIT_BF16, 6, 1e-12), (cg.PLAIN_FP64, None, 1e-12))
 
 CASES = {
     "medium": lambda: synth.make_config("medium"),
@@ -64,18 +66,17 @@ def test_both_forms_vs_oracle_at_full_size(name):
     _release()
     out = None
     try:
-        for prec in (cg.SPLIT_BF16, cg.PLAIN_FP64):
-            X, I = cg.build_integrals_device(sub, prec, out=out)
+        for prec, n_slices, tol in FORMS:
+            X, I = cg.build_integrals_device(sub, prec, n_slices=n_slices, out=out)
             out = (X, I)
             got_x = X.cpu().numpy()
             got_rows = I[torch.from_numpy(rows).to(I.device)].cpu().numpy()
             got_v = (I @ torch.from_numpy(v).to(I.device)).cpu().numpy()
             _release()
-            tol = TOL[prec]
             for what, a, b in (("X", got_x, X4[:3]), ("int_2e rows", got_rows, I_rows),
                                ("int_2e v", got_v, I_v)):
                 e = oracle.rel_err(a, b)
-                assert e["norm"] < tol and e["max"] < tol, (name, prec, what, e)
+                assert e["norm"] < tol and e["max"] < tol, (name, prec, n_slices, what, e)
     finally:
         del out
         _release()

@@ -83,6 +83,53 @@ def test_drop_in_env_selects_split(monkeypatch):
     _check(X, I, ref["X"], ref["int2e"])
 
 
+def test_drop_in_env_sets_slice_count(monkeypatch):
+    """CUTC_SLICES sets the split form's slice count for the drop-in; 6 slices bring it
+    within the plain form's 1e-12 of the reference's own outputs; a count outside 3..7
+    is refused."""
+    p, ref = load_case("tiny_spd")
+    monkeypatch.setenv("CUTC_PRECISION", "split")
+    dims = [int(v) for v in ref["dims"]]
+
+    def call():
+        X = np.zeros((3, p.n_grid1, p.n_ao ** 2))
+        I = np.zeros((p.n_ao ** 2, p.n_ao ** 2))
+        s = cg.cutc_int(*dims, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh, p.r1, p.wr1,
+                        p.r2, p.wr2, p.rn, p.aos1, p.aos2, p.c_bh, p.m_bh, p.n_bh, p.o_bh, X, I)
+        return s, X, I
+
+    monkeypatch.setenv("CUTC_SLICES", "6")
+    s, X, I = call()
+    assert s == 0, cg.last_error()
+    _check(X, I, ref["X"], ref["int2e"], tol=1e-12)
+    for bad in ("8", "2", "five", "6x"):
+        monkeypatch.setenv("CUTC_SLICES", bad)
+        s, _, _ = call()
+        assert s == cg.CUTC_ERR_INVALID, bad
+        assert "n_slices" in cg.last_error()
+
+
+@pytest.mark.parametrize("n_slices", [6, 7])
+def test_six_and_seven_slices_reach_fp64_class_errors(monkeypatch, n_slices):
+    """Builds of 6 and 7 slices: the pair contraction on the tensor cores with 6 slices
+    against the double-float pair kernel, and both against the oracle at 1e-12 (the
+    plain FP64 form's tolerance), with e-e coalescence and 20 nuclei (K = 80)."""
+    for n_nuc, coalesce in ((5, True), (20, False)):
+        p = synth.make_problem(n_nuc=n_nuc, n_ao=8, n_grid1=260, n_grid2=900, size_bh=9,
+                               seed=90 + n_nuc, a_en=1.1, a_ee=0.8, box=1.5 + 0.4 * n_nuc)
+        if coalesce:
+            p = synth.add_coalescence(p)
+        monkeypatch.delenv("CUTC_PAIR_DF", raising=False)
+        X1, I1 = cg.build_integrals(p, cg.SPLIT_BF16, n_slices=n_slices, x_components=4)
+        monkeypatch.setenv("CUTC_PAIR_DF", "1")
+        X2, I2 = cg.build_integrals(p, cg.SPLIT_BF16, n_slices=n_slices, x_components=4)
+        assert oracle.rel_err(X1, X2)["max"] < 1e-13
+        assert oracle.rel_err(I1, I2)["max"] < 1e-13
+        Xo, Io = oracle.cutc_int(p)
+        _check(X1[:3], I1, Xo, Io, tol=1e-12)
+        _check(X2[:3], I2, Xo, Io, tol=1e-12)
+
+
 def test_sparse_power_pair_kernel_matches_general(monkeypatch):
     """Exponents in {0, 2, 3, 4} select the sparse-power df pair kernel; the general
     kernel (CUTC_PAIR_DENSE) evaluates the same polynomials in another order."""
