@@ -1369,7 +1369,7 @@ extern "C" int cutc_plan(const cutc_options *opt, int n_grid1, int n_grid2, int 
     plan->footprint_bytes = build_footprint(R, budget);
     if (R.precision == CUTC_SPLIT_BF16) {
         const int64_t nkb = ((int64_t)n_grid2 + 31) / 32;
-        const int64_t per = split_k_blocks_per_launch(nkb * 32, opt->k_split);
+        const int64_t per = split_k_blocks_per_launch(nkb * 32, n_pairs(n_ao), opt->k_split);
         plan->x_launches_per_tile = (int)((nkb + per - 1) / per);
     } else {
         plan->x_launches_per_tile = 1;  // one FP64 GEMM launch over the four components

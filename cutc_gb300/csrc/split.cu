@@ -75,9 +75,16 @@ constexpr int kMaxKPerLaunch = 1 << 18;  // keeps every exact (hi, lo) sum below
 // X contraction of the 300-AO molecule (K = 200 000, 1500 r1 rows) took 1826 ms in one
 // launch and 1282 ms in five of 40 000; the medium one (K = 80 000) 1176 and 1168 ms
 // in one and two launches, and 1205 ms in three.  Over a long K loop the CTAs of a
-// wave probably drift apart and stop sharing their A and B tiles in L2.
+// wave probably drift apart and stop sharing their A and B tiles in L2.  With an A
+// operand of kBigM rows or more, launches of at most kLaunchKBigM pay: the 300-AO X
+// contraction (M = 45 150, K = 200 000) took 5141 ms per 6000 r1 rows in launches of
+// 40 000, 4995 in launches of 20 000 and 4971 in launches of 10 000, while the medium
+// one (M = 7260) was the same at 40 000 and 20 000 and 4 % slower at 10 000.
 constexpr int kLongK = 65536;
 constexpr int kLaunchK = 49152;
+constexpr int kBigM = 16384;
+constexpr int kLongKBigM = 32768;
+constexpr int kLaunchKBigM = 24576;
 constexpr uint32_t kTmemCols = 512;
 constexpr int kGroupM = 8;      // row tiles per raster group (A tiles shared through L2)
 
@@ -1096,13 +1103,15 @@ static int slice_cols(cudaStream_t st, const double *X, int64_t ld, int64_t k0, 
     return CUTC_OK;
 }
 
-int split_k_blocks_per_launch(int64_t K, int k_split)
+int split_k_blocks_per_launch(int64_t K, int64_t M, int k_split)
 {
     const int64_t nkb_total = (std::max<int64_t>(K, 1) + kBK - 1) / kBK;
     if (k_split > 0)
         return std::max(1, std::min(k_split, kMaxKPerLaunch) / kBK);
     const int64_t kt = nkb_total * kBK;
-    const int64_t launches = kt <= kLongK ? 1 : (kt + kLaunchK - 1) / kLaunchK;
+    const bool big = M >= kBigM;
+    const int64_t one = big ? kLongKBigM : kLongK, each = big ? kLaunchKBigM : kLaunchK;
+    const int64_t launches = kt <= one ? 1 : (kt + each - 1) / each;
     return (int)((nkb_total + launches - 1) / launches);
 }
 
@@ -1124,7 +1133,7 @@ static int gemm(cudaStream_t st, const Operand &A, const Operand &B, double alph
     CUTC_TRY(make_tmap(&ta, A.sl, (int64_t)S * A.Mpad, A.Kpad, kBM));
     CUTC_TRY(make_tmap(&tb, B.sl, (int64_t)S * B.Mpad, B.Kpad, Cfg::kBN));
     const int nkb_total = (int)(A.Kpad / kBK);
-    const int kb_per = split_k_blocks_per_launch(A.Kpad, k_split);
+    const int kb_per = split_k_blocks_per_launch(A.Kpad, A.M, k_split);
     if (A.Mpad % kBM || B.Mpad % Cfg::kBN) {
         cutc_set_error(CUTC_ERR_INVALID, "operand padding does not match the tile");
         return CUTC_ERR_INVALID;

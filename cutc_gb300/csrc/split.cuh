@@ -42,9 +42,10 @@ struct SplitPlan {
 
 // Device bytes per r1 row of an X tile (slices of G).
 size_t split_r1_row_bytes(const Request &R);
-// 32-wide K blocks per tensor-core launch of a contraction over K (k_split as in
-// cutc_options: 0 = one launch up to K = 65536, equal launches of <= 49152 beyond).
-int split_k_blocks_per_launch(int64_t K, int k_split);
+// 32-wide K blocks per tensor-core launch of a contraction over K with an A operand of
+// M rows (k_split as in cutc_options: 0 = one launch up to K = 65536, equal launches of
+// <= 49152 beyond; for M >= 16384 one launch up to 32768, launches of <= 24576 beyond).
+int split_k_blocks_per_launch(int64_t K, int64_t M, int k_split);
 // Device bytes per r1 row of an int_2e block (slices of its int_2e operands).
 size_t split_int2e_row_bytes(const Request &R);
 // Device bytes that do not depend on the tile size (the P slices).

@@ -94,12 +94,19 @@ def test_plan_without_budget_needs_a_device():
 
 def test_x_contraction_launches_per_tile():
     """Split form: one tensor-core launch up to K = n_grid2 = 65536, equal launches of
-    at most 49152 beyond (FP64 sums between them); an explicit k_split caps them."""
+    at most 49152 beyond (FP64 sums between them); with 16384 or more packed AO pairs
+    (the A operand's rows) one launch up to 32768 and launches of at most 24576 beyond;
+    an explicit k_split caps them."""
     budget = 8 << 30
     for n2, launches in ((12000, 1), (50000, 1), (65536, 1), (65537, 2), (80000, 2),
                          (120000, 3), (200000, 5)):
         info = cg.plan(500, n2, 20, 3, cg.SPLIT_BF16, 5, max_work_bytes=budget)
         assert info["x_launches_per_tile"] == launches, (n2, info)
+    # n_ao = 180: 16290 pairs; 181: 16471
+    for n_ao, n2, launches in ((180, 80000, 2), (181, 32768, 1), (181, 32769, 2),
+                               (181, 80000, 4), (300, 200000, 9)):
+        info = cg.plan(500, n2, n_ao, 3, cg.SPLIT_BF16, 5, max_work_bytes=budget)
+        assert info["x_launches_per_tile"] == launches, (n_ao, n2, info)
     assert cg.plan(500, 80000, 20, 3, cg.SPLIT_BF16, 5, max_work_bytes=budget,
                    k_split=16384)["x_launches_per_tile"] == 5
     assert cg.plan(500, 200000, 20, 3, cg.SPLIT_BF16, 5, max_work_bytes=budget,
