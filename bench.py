@@ -47,6 +47,7 @@ from cutc_gb300 import synth  # noqa: E402
 
 METRIC = "TC integral builds/s (split-precision vs FP64 at 1e-10 rel err)"
 UNIT = "builds/s"
+FP64_CLASS_SLICES = 6        # the split form's slice count with the plain form's error class
 CPU_SAMPLE_ROWS = 256       # per step of --impl reference: about 6 s of oracle work on 16 cores
 CPU_BASELINE_ROWS = 384     # the cpu_baseline leg: about 10 s; smaller samples underrate the
                             # CPU (48 rows gave 0.00096 builds/s, 256 rows 0.00168)
@@ -116,6 +117,42 @@ def cuda_ms(fn, stream=None):
     e1.record(s)
     torch.cuda.synchronize()
     return e0.elapsed_time(e1)
+
+
+def fp64_class_leg(cg, p, n_slices, steps=2):
+    """The split form at n_slices (6: the plain form's error class) on the full
+    workload, device-resident, timed with CUDA events after one warm-up build."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    nA2 = p.n_ao ** 2
+    stream = torch.cuda.Stream(device=dev)
+    opt = cg.options(cg.SPLIT_BF16, n_slices, p.a_en, p.a_ee, 3, True, 0, stream.cuda_stream)
+    dr = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in p.arrays().items()}
+    Xd = torch.empty((3, p.n_grid1, nA2), dtype=torch.float64, device=dev)
+    Id = torch.empty((nA2, nA2), dtype=torch.float64, device=dev)
+
+    def build():
+        s = cg.cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                           dr["r1"], dr["wr1"], dr["r2"], dr["wr2"], dr["rn"], dr["aos1"],
+                           dr["aos2"], dr["c_bh"], dr["m_bh"], dr["n_bh"], dr["o_bh"], Xd, Id, None)
+        if s != cg.CUTC_OK:
+            raise cg.CutcError(s, cg.last_error())
+
+    build()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        build()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    del dr, Xd, Id
+    release_device()
+    return {"value": 1e3 / ms, "unit": UNIT, "ms_per_build": ms, "n_slices": n_slices,
+            "steps": steps, "note": "device-resident builds of the full workload in the split "
+                                    "form at %d slices; its error against the oracle is the "
+                                    "accuracy object's split_%d_slices entry" % (n_slices, n_slices)}
 
 
 def plain_rate_estimate(cg, p, sizes):
@@ -411,7 +448,9 @@ def run_ours(args):
     drop_in = None
     if p.a_en == 1.0 and p.a_ee == 1.0:  # cutc_int fixes them, like the reference
         prev = os.environ.get("CUTC_PRECISION")
+        prev_slices = os.environ.get("CUTC_SLICES")
         os.environ["CUTC_PRECISION"] = "split" if prec == cg.SPLIT_BF16 else "plain"
+        os.environ["CUTC_SLICES"] = str(args.slices)
         ha = {k: np.ascontiguousarray(v) for k, v in p.arrays().items()}
         Xp = np.empty((3, p.n_grid1, nA2))
         Ip = np.empty((nA2, nA2))
@@ -435,11 +474,13 @@ def run_ours(args):
         drop_in = {"value": whole_job_rate(world, drop_steps, drop_s), "unit": UNIT,
                    "steps": drop_steps,
                    "entry": "cutc_int with its launch integers, pageable numpy arrays in and "
-                            "out, CUTC_PRECISION=%s" % os.environ["CUTC_PRECISION"]}
-        if prev is None:
-            del os.environ["CUTC_PRECISION"]
-        else:
-            os.environ["CUTC_PRECISION"] = prev
+                            "out, CUTC_PRECISION=%s, CUTC_SLICES=%s"
+                            % (os.environ["CUTC_PRECISION"], os.environ["CUTC_SLICES"])}
+        for key, old in (("CUTC_PRECISION", prev), ("CUTC_SLICES", prev_slices)):
+            if old is None:
+                del os.environ[key]
+            else:
+                os.environ[key] = old
         del Xp, Ip, ha
         log("drop-in cutc_int, pageable arrays: %.3f builds/s" % drop_in["value"])
     log("e2e: %.3f builds/s" % e2e_value)
@@ -502,8 +543,12 @@ def run_ours(args):
             acc = {"sample": "%d of %d r1 rows spread over the grid; both forms against the FP64 "
                              "oracle (oracle/, C restatement of the reference's kernels + numpy "
                              "DGEMM)" % (sub.n_grid1, p.n_grid1)}
-            for name, pr in (("split", cg.SPLIT_BF16), ("plain", cg.PLAIN_FP64)):
-                X, I = cg.build_integrals(sub, pr, n_slices=args.slices if pr else None)
+            forms = [("split", cg.SPLIT_BF16, args.slices), ("plain", cg.PLAIN_FP64, None)]
+            if prec == cg.SPLIT_BF16 and args.slices < FP64_CLASS_SLICES:
+                forms.append(("split_%d_slices" % FP64_CLASS_SLICES, cg.SPLIT_BF16,
+                              FP64_CLASS_SLICES))
+            for name, pr, ns in forms:
+                X, I = cg.build_integrals(sub, pr, n_slices=ns)
                 acc[name] = {"X_vs_oracle": rel(X, Xo[:3]), "int2e_vs_oracle": rel(I, Io)}
                 del X, I
             out["accuracy"] = acc
@@ -512,6 +557,10 @@ def run_ours(args):
     if one_gpu and not args.skip_accuracy:
         log("plain FP64 rate")
         out["plain_fp64"] = guarded(plain_rate_estimate, cg, p, (256, 512))
+        if prec == cg.SPLIT_BF16 and args.slices < FP64_CLASS_SLICES:
+            log("split form at %d slices" % FP64_CLASS_SLICES)
+            out["split_%d_slices" % FP64_CLASS_SLICES] = guarded(fp64_class_leg, cg, p,
+                                                                  FP64_CLASS_SLICES)
     if one_gpu and not args.skip_large:
         log("large workload on r1 samples")
         out["large"] = guarded(large_leg, cg, args, 1, 1, not args.skip_accuracy)
