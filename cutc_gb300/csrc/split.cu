@@ -937,7 +937,11 @@ __global__ void slice_kernel(Src src, int M, int64_t K, int64_t Kpad, int Mpad,
         for (int q = 0; q < 4; q++) {
             if constexpr (Src::kDoubleFloat) {
                 const float2 v = (r < M && k + q < K) ? src.pair(r, k + q) : make_float2(0.f, 0.f);
-                digits_of<S>(digits::scaled_round_df<S>(v.x, v.y, e), d[q]);
+                float qf[S];
+                digits::digits_df_fp32<S>(v.x, v.y, e, qf);
+#pragma unroll
+                for (int s = 0; s < S; s++)
+                    d[q][s] = __float2bfloat16_rn(__fmul_rn(qf[s], exp2f((float)(-8 - 9 * s))));
             } else {
                 const double x = (r < M && k + q < K) ? src(r, k + q) : 0.0;
                 split_digits<S>(x, e, d[q]);

@@ -7,7 +7,11 @@
 //     scaled_round on hi + lo whenever that sum is exact in FP64, on random values
 //     over a wide exponent range, on exact ties and on the largest value of a row;
 //   * digits_int cuts t into digits with t = sum_s q_s 2^(9 (S - 1 - s)),
-//     q_s in [-256, 255] for s > 0 and |q_0| <= 256.
+//     q_s in [-256, 255] for s > 0 and |q_0| <= 256;
+//   * digits_df_fp32 cuts the double-float (hi, lo) in FP32 into integer digits
+//     q_s in [-256, 256] whose value sum_s q_s 2^(9 (S - 1 - s)) is within
+//     1/2 + 2^-16 of (hi + lo) 2^(F - e) (checked in long double), i.e. within one
+//     of scaled_round_df's t.
 // Prints "ok <cases> <double-float cases>" and exits 0, or reports the first failure
 // and exits 1.
 #include <cmath>
@@ -39,6 +43,23 @@ static void fail(const char *what, int S, double x, float hi, float lo, int e, l
 }
 
 template <int S>
+static void check_fp32_digits(float hi, float lo, int e, double x)
+{
+    constexpr int F = 8 + 9 * (S - 1);
+    float q[S];
+    digits_df_fp32<S>(hi, lo, e, q);
+    long long back = 0;
+    for (int s = 0; s < S; s++) {
+        if (q[s] != std::rint(q[s]) || q[s] < -256.0f || q[s] > 256.0f)
+            fail("fp32 digit", S, x, hi, lo, e, (long long)q[s], s);
+        back = back * 512 + (long long)q[s];
+    }
+    const long double v = std::ldexp((long double)x, F - e);
+    if (std::fabs((double)((long double)back - v)) > 0.5 + std::ldexp(1.0, -16))
+        fail("fp32 digits value", S, x, hi, lo, e, back, 0);
+}
+
+template <int S>
 static void check_value(double x, int e)
 {
     constexpr int F = 8 + 9 * (S - 1);
@@ -67,6 +88,7 @@ static void check_value(double x, int e)
         const long long u = scaled_round_df<S>(hi, lo, e);
         if (u != t)
             fail("scaled_round_df", S, x, hi, lo, e, u, t);
+        check_fp32_digits<S>(hi, lo, e, x);
         df_cases++;
     }
     cases++;
@@ -105,6 +127,17 @@ static void run()
             continue;
         check_value<S>(x, e);
         check_value<S>(-x, e);
+    }
+    // rows at the ends of the FP32 range: 2^(8 - e) outside [2^-126, 2^127] (the FP32
+    // cut scales in two steps), subnormal hi
+    for (int i = 0; i < 20000; i++) {
+        const int ex = (i & 1) ? 100 + (int)(next_u64() % 27) : -149 + (int)(next_u64() % 40);
+        double x = (2.0 * uniform() - 1.0) * std::ldexp(1.0, ex);
+        x = (double)(float)x;  // exactly one float, lo = 0
+        if (x == 0.0)
+            continue;
+        const int e = row_exp(x) + (int)(next_u64() % 3);
+        check_value<S>(x, e);
     }
     // the row maximum itself and values just below a power of two
     for (int k = -30; k <= 30; k++) {
