@@ -34,6 +34,16 @@ struct PairArgs {
 // FP64 (where they are exact) instead of double-float.
 constexpr float kNearPairR2 = 1.0e-4f;
 
+// The high word of the FP64 form of a non-negative float given by its bits (float
+// subnormals count as 2^-126): the row-maximum word the slicers read.  It is a
+// non-decreasing function of the bits, so the maximum of a warp's words is the word of
+// the warp's largest bits, and one conversion after the reduction serves the warp.
+__device__ __forceinline__ unsigned rmax_word(unsigned fb)
+{
+    const unsigned ef = fb >> 23;
+    return fb == 0u ? 0u : ef == 0u ? (897u << 20) : ((ef + 896u) << 20) | ((fb & 0x7fffffu) >> 3);
+}
+
 // Arguments of the double-float pair kernel (split form).
 struct PairDfArgs {
     int i0, n1b, n2, nN;

@@ -272,11 +272,7 @@ pair_df_kernel(PairDfArgs P)
 #pragma unroll
             for (int c = 0; c < 4; c++) {
                 const unsigned fb = __float_as_uint(w4[c].x) & 0x7fffffffu;
-                const unsigned ef = fb >> 23;
-                const unsigned hw = fb == 0u ? 0u
-                                  : ef == 0u ? (897u << 20)
-                                             : ((ef + 896u) << 20) | ((fb & 0x7fffffu) >> 3);
-                const unsigned m = __reduce_max_sync(mask, hw);
+                const unsigned m = rmax_word(__reduce_max_sync(mask, fb));
                 if (leader && m)
                     atomicMax(&P.rmax[(int64_t)c * P.n1b + row0 + r], (unsigned long long)m << 32);
             }

@@ -684,17 +684,19 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             const int i = (t_begin + q) * Cfg::kPts + pt;  // r1 row of the tile
             if (i >= P.n1b)
                 continue;
-            // V_c = 2^(ea + eb_c) ((H + L) + L2): TwoSum of H and L, then the rest
+            // V_c 2^-ea = 2^eb_c ((H + L) + L2): TwoSum of H and L, then the rest.  The F
+            // rows' scale 2^ea, a power of two common to the 16 values, multiplies the
+            // results instead (the polynomial is linear in V, and power-of-two scaling
+            // commutes with the double-float arithmetic).
             df::D V[16];
-            const float *scr = Q.bscale + (int64_t)i * 16;
+            const float *scr = Q.bscale + (int64_t)i * 16;  // 16-float aligned rows
 #pragma unroll
             for (int k = 0; k < 8; k++) {
                 const uint64_t sm = tc::f2_add(H[k], L[k]);
                 const uint64_t bb = tc::f2_sub(sm, H[k]);
                 uint64_t e = tc::f2_add(tc::f2_sub(H[k], tc::f2_sub(sm, bb)), tc::f2_sub(L[k], bb));
                 e = tc::f2_add(e, L2[k]);
-                const uint64_t sc = tc::f2_pack(__float_as_uint(sa * scr[2 * k]),
-                                                __float_as_uint(sa * scr[2 * k + 1]));
+                const uint64_t sc = *reinterpret_cast<const uint64_t *>(scr + 2 * k);
                 const uint64_t hs = tc::f2_mul(sm, sc), ls = tc::f2_mul(e, sc);
                 V[2 * k] = df::make(tc::f2_lo(hs), tc::f2_lo(ls));
                 V[2 * k + 1] = df::make(tc::f2_hi(hs), tc::f2_hi(ls));
@@ -743,6 +745,9 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 ux = df::fma(dudg, gx, ux);
                 uy = df::fma(dudg, gy, uy);
                 uz = df::fma(dudg, gz, uz);
+                ux = df::make(__fmul_rn(ux.hi, sa), __fmul_rn(ux.lo, sa));
+                uy = df::make(__fmul_rn(uy.hi, sa), __fmul_rn(uy.lo, sa));
+                uz = df::make(__fmul_rn(uz.hi, sa), __fmul_rn(uz.lo, sa));
                 const df::D n2v = df::add(df::add(df::sqr(ux), df::sqr(uy)), df::sqr(uz));
                 const df::D lv = df::mul_f(n2v, -0.5f);
                 w4[0] = make_float2(ux.hi, ux.lo);
@@ -761,11 +766,7 @@ pair_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
                         const unsigned fb = __float_as_uint(w4[c].x) & 0x7fffffffu;
-                        const unsigned ef = fb >> 23;
-                        const unsigned hw = fb == 0u ? 0u
-                                          : ef == 0u ? (897u << 20)
-                                                     : ((ef + 896u) << 20) | ((fb & 0x7fffffu) >> 3);
-                        const unsigned m = __reduce_max_sync(mask, hw);
+                        const unsigned m = rmax_word(__reduce_max_sync(mask, fb));
                         if (leader && m)
                             atomicMax(&P.rmax[(int64_t)c * P.n1b + i], (unsigned long long)m << 32);
                     }
