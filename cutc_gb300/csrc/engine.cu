@@ -508,6 +508,7 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     // ---- inputs on the device --------------------------------------------
     const double *d_r1 = nullptr, *d_wr1 = nullptr, *d_r2 = nullptr, *d_wr2 = nullptr;
     const double *d_rn = nullptr, *d_aos1 = nullptr, *d_aos2v = nullptr;
+    bool aos1_deferred = false;
     void *p;
     auto put = [&](int slot, const void *h, size_t bytes, const double **dst) -> int {
         CUTC_TRY(W.get(slot, bytes, &p));
@@ -528,15 +529,12 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         CUTC_TRY(put(S_R2, R.r2, 3 * (size_t)n2 * 8, &d_r2));
         CUTC_TRY(put(S_WR2, R.wr2, (size_t)n2 * 8, &d_wr2));
         CUTC_TRY(put(S_RN, R.rn, 3 * (size_t)nN * 8, &d_rn));
-        if (R.aos1 && R.ld1 > n1) {
-            // an r1 window of a larger grid: its 4 nA columns of n1 points, packed
+        if (R.aos1 && !R.x_only) {
+            // the AO values on r1, the largest input, are read only by the int_2e blocks:
+            // they are copied on the transfer stream once the first tile is queued
             CUTC_TRY(W.get(S_AOS1, 4 * (size_t)n1 * nA * 8, &p));
-            CUTC_CUDA_TRY(cudaMemcpy2DAsync(p, (size_t)n1 * 8, R.aos1, (size_t)R.ld1 * 8,
-                                            (size_t)n1 * 8, 4 * (size_t)nA,
-                                            cudaMemcpyHostToDevice, st));
             d_aos1 = (const double *)p;
-        } else if (R.aos1) {
-            CUTC_TRY(put(S_AOS1, R.aos1, 4 * (size_t)n1 * nA * 8, &d_aos1));
+            aos1_deferred = true;
         }
         // only the value component of aos_data2 is used (src/long_range_integ.cu:30-35)
         if (R.aos2)
@@ -779,6 +777,18 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         }
         if (tev)
             CUTC_CUDA_TRY(cudaEventRecord(tev[1], st));
+        if (tile == 0 && aos1_deferred) {
+            // (from pageable memory the call returns once staged: the GPU is busy meanwhile)
+            void *dst = const_cast<double *>(d_aos1);
+            if (R.ld1 > n1)  // an r1 window of a larger grid: its 4 nA columns, packed
+                CUTC_CUDA_TRY(cudaMemcpy2DAsync(dst, (size_t)n1 * 8, R.aos1, (size_t)R.ld1 * 8,
+                                                (size_t)n1 * 8, 4 * (size_t)nA,
+                                                cudaMemcpyHostToDevice, E->xfer));
+            else
+                CUTC_CUDA_TRY(cudaMemcpyAsync(dst, R.aos1, 4 * (size_t)n1 * nA * 8,
+                                              cudaMemcpyHostToDevice, E->xfer));
+            CUTC_CUDA_TRY(cudaEventRecord(E->ev[6], E->xfer));
+        }
 
         // X rows of the tile into the block:
         //   Xt[(m blk_rows + ib + i) np + p] = sum_g P[p n2 + g] G[m plane + i n2 + g]
@@ -805,6 +815,8 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         if (i0 + nb == blk0 + blk_rows && !R.x_only) {
             const int K = blk_rows;
             const double *w1 = d_wr1 + blk0, *a1 = d_aos1 + blk0;
+            if (aos1_deferred && first_blk)
+                CUTC_CUDA_TRY(cudaStreamWaitEvent(st, E->ev[6], 0));
             if (R.precision == CUTC_PLAIN_FP64) {
                 const bool keep =
                     K == n1 && R.mol_tag && E->tag_i == R.mol_tag && E->tag_i_buf == d_S0;
