@@ -649,15 +649,18 @@ def guarded(fn, *a):
 # ---------------------------------------------------------------------------
 # the large workload: r1 samples of the full molecule and grids
 # ---------------------------------------------------------------------------
-def large_leg(cg, args, warmup, steps, with_accuracy, sizes=(3000, 6000)):
-    """Large workload (n_ao=300, n_grid2=200,000) timed on two r1 samples spread
-    over the 60,000-point r1 grid and extrapolated linearly in n_grid1.
+def large_leg(cg, args, warmup, steps, with_accuracy, sizes=(3000, 6000), full_build=True):
+    """Large workload (n_ao=300, n_grid2=200,000): one full device-resident build of
+    the 60,000-point r1 grid with int_2e returned and X formed on the device but not
+    copied out, and, as a cross-check, two r1 samples spread over the grid,
+    extrapolated linearly in n_grid1.
 
     A full build's outputs (X: 130 GB, int_2e: 65 GB) do not fit the GPU host's
-    memory beside each other, so the full grid is not built in one call; the
-    device-resident cost of a build is exactly linear in the r1 rows it holds
-    (every r1 tile does the same work), plus a fixed part (P slices, int_2e
-    assembly), which the two samples separate.
+    memory beside each other, nor the device beside the working set, so the full
+    build returns int_2e alone; the samples return X as well.  The device-resident
+    cost of a build is linear in the r1 rows it holds (every r1 tile does the same
+    work) plus a fixed part (P slices, int_2e assembly), which the two samples
+    separate.
     """
     import torch
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -711,12 +714,37 @@ def large_leg(cg, args, warmup, steps, with_accuracy, sizes=(3000, 6000)):
         samples.append({"r1_rows": ns, "ms_per_build": ms, "r1_tiles": tiles})
         log("large: %d rows: %.1f ms per build" % (ns, ms))
         del dr, Xd
+    full = None
+    if full_build:
+        # the whole r1 grid in one call: X (130 GB) is formed on the device in the
+        # contractions' packed layout but not returned, int_2e (65 GB) stays on the device
+        log("large: one full build, int_2e returned, X not copied out")
+        dr = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in p.arrays().items()}
+        torch.cuda.synchronize(dev)
+        st = cg.Stats()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s = cg.cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                           dr["r1"], dr["wr1"], dr["r2"], dr["wr2"], dr["rn"], dr["aos1"],
+                           dr["aos2"], dr["c_bh"], dr["m_bh"], dr["n_bh"], dr["o_bh"], None, Id, st)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        if s != cg.CUTC_OK:
+            raise cg.CutcError(s, cg.last_error())
+        full = {"ms_per_build": e0.elapsed_time(e1), "r1_tiles": st.n_r1_tiles,
+                "ms_x_gemm": st.ms_x_gemm, "ms_pair": st.ms_pair, "ms_int2e": st.ms_int2e,
+                "note": "one device-resident build of all %d r1 rows (no warm-up beyond the "
+                        "samples'), int_2e returned on the device, X formed but not copied "
+                        "out (cutc_int_ex with int2_grad1_u12_ao = NULL)" % p.n_grid1}
+        log("large: full build %.0f ms" % full["ms_per_build"])
+        del dr
     clocks = sampler.stop()
     del Id
     release_device()
     (n_a, n_b), (t_a, t_b) = sizes, (samples[0]["ms_per_build"], samples[1]["ms_per_build"])
     slope = (t_b - t_a) / (n_b - n_a)
-    t_full = t_b + slope * (p.n_grid1 - n_b)
+    t_proj = t_b + slope * (p.n_grid1 - n_b)
+    t_full = full["ms_per_build"] if full else t_proj
     value = 1e3 / t_full
 
     peaks, peak_kind = measured_peaks()
@@ -729,9 +757,10 @@ def large_leg(cg, args, warmup, steps, with_accuracy, sizes=(3000, 6000)):
     executed = achieved * packed * n_products if n_products else None
     out = {"value": value, "unit": UNIT, "ms_per_build": t_full,
            "workload": workload_desc("large", p), "precision": args.precision,
+           "full_build": full,
            "projection": "device-resident builds on %d and %d r1 rows spread over the r1 grid "
-                         "(%d warm-up, %d timed each), extrapolated linearly to n_grid1=%d"
-                         % (n_a, n_b, warmup, steps, p.n_grid1),
+                         "(%d warm-up, %d timed each), extrapolated linearly to n_grid1=%d: "
+                         "%.0f ms per build" % (n_a, n_b, warmup, steps, p.n_grid1, t_proj),
            "samples": samples, "gpu_launches": launches, "clocks": clocks,
            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
                         "unit": "TFLOP/s", "frac": achieved / peak,

@@ -289,8 +289,12 @@ static int validate(const Request &R)
         cutc_set_error(CUTC_ERR_INVALID, "n_ao=%d too large", R.nA);
         return CUTC_ERR_INVALID;
     }
-    const void *ptrs[] = {R.r1, R.r2, R.wr2, R.rn, R.X, R.x_only ? R.X : R.wr1,
-                          R.x_only ? R.X : R.I};
+    if (R.x_only && R.i_only) {
+        cutc_set_error(CUTC_ERR_INVALID, "NULL X and int_2e outputs: nothing to build");
+        return CUTC_ERR_INVALID;
+    }
+    const void *ptrs[] = {R.r1, R.r2, R.wr2, R.rn, R.i_only ? R.I : R.X,
+                          R.x_only ? R.X : R.wr1, R.x_only ? R.X : R.I};
     for (const void *p : ptrs)
         if (!p) {
             cutc_set_error(CUTC_ERR_INVALID, "NULL array argument");
@@ -391,7 +395,7 @@ static size_t fixed_bytes(const Request &R)
 static size_t r1_row_bytes(const Request &R)
 {
     size_t b = 4 * (size_t)R.n2 * 8 + (size_t)R.nN * sizeof(NucTerm);
-    if (!(R.device_pointers || R.out_device))
+    if (!(R.device_pointers || R.out_device) && !R.i_only)
         b += 2 * (size_t)R.x_components * R.nA * R.nA * 8;
     if (R.precision == CUTC_SPLIT_BF16)
         b += split_r1_row_bytes(R) + pair_df_poly_bytes(6, 1, R.nN) + split_pair_row_bytes(R);
@@ -623,8 +627,10 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     const int slab = int2e_slab_cols(nA);
     if (!out_dev) {
         for (int k = 0; k < 2; k++) {
-            CUTC_TRY(W.get(S_XOUT + k, (size_t)R.x_components * n1t * nA2 * 8, &p));
-            stage_x[k] = (double *)p;
+            if (!R.i_only) {
+                CUTC_TRY(W.get(S_XOUT + k, (size_t)R.x_components * n1t * nA2 * 8, &p));
+                stage_x[k] = (double *)p;
+            }
             if (!R.x_only) {
                 CUTC_TRY(W.get(S_IOUT + k, (size_t)slab * nA2 * 8, &p));
                 stage_i[k] = (double *)p;
@@ -682,7 +688,7 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     StreamsDrain drain{st, E->xfer};
     cudaEvent_t ready[2] = {E->ev[3], E->ev[4]}, done[2] = {E->ev[9], E->ev[10]};
     bool busy[2] = {false, false};
-    const bool x_direct = out_dev || async_host_ptr(R.X);
+    const bool x_direct = out_dev || R.i_only || async_host_ptr(R.X);
     const bool i_direct = out_dev || R.x_only || async_host_ptr(R.I);
     double *hpin_x[2] = {nullptr, nullptr}, *hpin_i[2] = {nullptr, nullptr};
     for (int k = 0; k < 2 && !out_dev; k++) {
@@ -845,7 +851,9 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
             CUTC_CUDA_TRY(cudaEventRecord(tev[5], st));
 
         // the tile's X rows in the reference layout X[m][i][b][a]
-        if (out_dev) {
+        if (R.i_only) {
+            // X stays packed in the int_2e block and is not returned
+        } else if (out_dev) {
             for (int m = 0; m < R.x_components; m++)
                 CUTC_TRY(launch_expand_pairs(st, nb, nA, d_Xt + ((int64_t)m * blk_rows + ib) * np,
                                              np, R.X + ((int64_t)m * n1 + i0) * nA2));
@@ -861,13 +869,14 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
             if (tile > 0)
                 CUTC_TRY(finish_x(tile - 1));
         }
-        note_launches(R.x_components);
+        if (!R.i_only)
+            note_launches(R.x_components);
         if (i0 + nb == blk0 + blk_rows) {  // next block
             blk0 += blk_rows;
             blk_rows = (int)std::min<int64_t>(kb, n1 - blk0);
         }
     }
-    if (!out_dev && n_tiles > 0)
+    if (!out_dev && n_tiles > 0 && !R.i_only)
         CUTC_TRY(finish_x(n_tiles - 1));
     CUTC_CUDA_TRY(cudaEventRecord(E->ev[5], st));
 
@@ -1069,6 +1078,7 @@ extern "C" int cutc_int_ex(const cutc_options *opt, int n_grid1, int n_grid2, in
     R.c_bh = c_bh; R.m_bh = m_bh; R.n_bh = n_bh; R.o_bh = o_bh;
     R.X = int2_grad1_u12_ao; R.I = int_2e_ao;
     R.x_only = int_2e_ao == nullptr;
+    R.i_only = int2_grad1_u12_ao == nullptr;
     if (opt->r1_begin != 0 || opt->r1_end != 0) {
         // an r1 shard: the window's points of the full arrays
         if (opt->r1_begin < 0 || opt->r1_end <= opt->r1_begin || opt->r1_end > n_grid1) {

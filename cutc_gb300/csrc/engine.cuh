@@ -73,6 +73,7 @@ struct Request {
     const cutc_basis *basis = nullptr;  // evaluates aos1 / aos2 when those are NULL
     uint64_t mol_tag = 0;  // non-zero: molecule arrays identical to earlier builds with this tag
     int x_only = 0;        // X alone (int_2e output NULL): wr1, aos1 and I are not used
+    int i_only = 0;        // int_2e alone (X output NULL): X is formed but not returned
     cudaStream_t stream = nullptr;
     int n1 = 0, n2 = 0, nA = 0, nN = 0, nB = 0;
     int64_t ld1 = 0;  // leading dimension (points) of aos1 when it is a window of a larger grid

@@ -123,7 +123,10 @@ void cutc_default_options(cutc_options *opt);
  * (inputs and outputs) are device pointers on the current device and no
  * host<->device copies are made.  stats may be NULL.  int_2e_ao may be NULL:
  * then only X is built (opt->x_components of them), and wr1 and aos_data1 are
- * not read and may be NULL too.
+ * not read and may be NULL too.  int2_grad1_u12_ao may be NULL instead: then
+ * only int_2e is returned (X is formed on the device in the packed layout the
+ * contractions use and is not expanded or copied out), for builds whose X would
+ * not fit beside the working set or is not needed.
  */
 int cutc_int_ex(const cutc_options *opt,
                 int n_grid1, int n_grid2, int n_ao, int n_nuc, int size_bh,

@@ -167,3 +167,38 @@ def test_registered_outputs_match_pageable(tile_rows):
         assert np.array_equal(X, Xh) and np.array_equal(I, Ih)
     finally:
         blk.close()
+
+
+@pytest.mark.parametrize("prec", [cg.PLAIN_FP64, cg.SPLIT_BF16])
+def test_int2e_only_builds_match_full_builds(prec, tile_rows):
+    """A NULL X output returns int_2e alone (X is formed on the device and not copied
+    out): the same int_2e bit for bit as a full build, from host and from device
+    arrays, over several tiles; both outputs NULL is refused."""
+    import torch
+    p = _problem()
+    tile_rows(100)
+    X, I = cg.build_integrals(p, prec)
+    h = {k: np.ascontiguousarray(v) for k, v in p.arrays().items()}
+    opt = cg.options(prec, None, p.a_en, p.a_ee, 3, False, 0, None)
+    Ih = np.full((p.n_ao ** 2, p.n_ao ** 2), np.nan)
+    st = cg.Stats()
+    s = cg.cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                       h["r1"], h["wr1"], h["r2"], h["wr2"], h["rn"], h["aos1"], h["aos2"],
+                       h["c_bh"], h["m_bh"], h["n_bh"], h["o_bh"], None, Ih, st)
+    assert s == 0, cg.last_error()
+    assert st.n_r1_tiles >= 5
+    assert np.array_equal(Ih, I)
+    dev = torch.device("cuda", 0)
+    d = {k: torch.from_numpy(v).to(dev) for k, v in h.items()}
+    Id = torch.full((p.n_ao ** 2, p.n_ao ** 2), float("nan"), dtype=torch.float64, device=dev)
+    optd = cg.options(prec, None, p.a_en, p.a_ee, 3, True, 0, None)
+    s = cg.cutc_int_ex(optd, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                       d["r1"], d["wr1"], d["r2"], d["wr2"], d["rn"], d["aos1"], d["aos2"],
+                       d["c_bh"], d["m_bh"], d["n_bh"], d["o_bh"], None, Id)
+    assert s == 0, cg.last_error()
+    torch.cuda.synchronize()
+    assert np.array_equal(Id.cpu().numpy(), I)
+    s = cg.cutc_int_ex(opt, p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, p.size_bh,
+                       h["r1"], h["wr1"], h["r2"], h["wr2"], h["rn"], h["aos1"], h["aos2"],
+                       h["c_bh"], h["m_bh"], h["n_bh"], h["o_bh"], None, None)
+    assert s == cg.CUTC_ERR_INVALID
