@@ -21,7 +21,8 @@
 //   * cutc_int_bh is the FP64 pair kernel of the plain form, on the r2 window
 //     and strides the reference's layout asks for;
 //   * get_int2_grad1_u12_ao is the streamed X build of cutc_int_ex (r1 tiles,
-//     packed AO pairs; plain FP64 unless CUTC_PRECISION=split) without int_2e;
+//     packed AO pairs; plain FP64 unless CUTC_PRECISION=split, with CUTC_SLICES
+//     slices) without int_2e;
 //   * get_int_2e_ao contracts the caller's full X (it need not be symmetric in
 //     the AO pair) against the short-range products in r1 blocks sized to a
 //     byte budget, with the FP64 DMMA GEMM accumulating in FP64, then adds A^T.
@@ -171,6 +172,18 @@ static int precision_from_env()
     return (prec && strcmp(prec, "split") == 0) ? CUTC_SPLIT_BF16 : CUTC_PLAIN_FP64;
 }
 
+// CUTC_SLICES as cutc_int reads it: a malformed or out-of-range count is passed on
+// for the build's own validation to refuse
+static int slices_from_env(int fallback)
+{
+    const char *sl = getenv("CUTC_SLICES");
+    if (!sl || !*sl)
+        return fallback;
+    char *end = nullptr;
+    const long v = strtol(sl, &end, 10);
+    return (*end == '\0' && v >= 0 && v <= 64) ? (int)v : -1;
+}
+
 }  // namespace cutc
 
 using namespace cutc;
@@ -258,6 +271,8 @@ extern "C" void get_int2_grad1_u12_ao(cutc_dim3 dimGrid, cutc_dim3 dimBlock, int
         return;
     Request R{};
     R.precision = precision_from_env();
+    if (R.precision == CUTC_SPLIT_BF16)
+        R.n_slices = slices_from_env(R.n_slices);
     R.x_components = 4;  // the reference's device array holds all four (m = 3: -1/2 |grad u|^2)
     R.device_pointers = 1;
     R.x_only = 1;

@@ -109,11 +109,15 @@ def test_cutc_int_bh_rejects_launch_dims_like_cutc_int():
     assert (G.cpu().numpy() == 7.0).all()
 
 
-@pytest.mark.parametrize("precision", ["plain", "split"])
+@pytest.mark.parametrize("precision", ["plain", "split", "split6"])
 def test_get_int2_grad1_u12_ao_all_four_components(precision, monkeypatch):
+    """Both forms, and the split form at 6 slices (CUTC_SLICES) at the plain form's
+    tolerance."""
     import torch
-    if precision == "split":
+    if precision != "plain":
         monkeypatch.setenv("CUTC_PRECISION", "split")
+    if precision == "split6":
+        monkeypatch.setenv("CUTC_SLICES", "6")
     p = _problem()
     nA2, n1 = p.n_ao ** 2, p.n_grid1
     X = torch.full((4, n1, nA2), float("nan"), dtype=torch.float64, device="cuda")
@@ -123,8 +127,27 @@ def test_get_int2_grad1_u12_ao_all_four_components(precision, monkeypatch):
                             p.size_bh, *_ptrs(mol), X.data_ptr())
     _sync_ok()
     Xo = oracle.x_block(p, oracle.long_range(p), 0, n1)
-    tol = 1e-12 if precision == "plain" else 1e-10
+    tol = 1e-10 if precision == "split" else 1e-12
     assert oracle.rel_err(X.cpu().numpy(), Xo)["max"] < tol, cg.last_error()
+
+
+def test_get_int2_grad1_u12_ao_refuses_a_bad_slice_count(monkeypatch):
+    import torch
+    monkeypatch.setenv("CUTC_PRECISION", "split")
+    monkeypatch.setenv("CUTC_SLICES", "9")
+    p = _problem()
+    X = torch.full((4, p.n_grid1, p.n_ao ** 2), 7.0, dtype=torch.float64, device="cuda")
+    L = cg.load()
+    mol = [_dev(a) for a in (p.r1, p.r2, p.wr2, p.rn, p.aos2, p.c_bh, p.m_bh, p.n_bh, p.o_bh)]
+    # a launch geometry error first, so that the message checked below is this call's
+    L.get_int2_grad1_u12_ao(cg.Dim3(8, 8, 1), cg.Dim3(2048, 1, 1), p.n_grid1, p.n_grid2, p.n_ao,
+                            p.n_nuc, p.size_bh, *_ptrs(mol), X.data_ptr())
+    assert "n_slices" not in cg.last_error()
+    L.get_int2_grad1_u12_ao(cg.Dim3(8, 8, 1), cg.Dim3(32, 8, 1), p.n_grid1, p.n_grid2, p.n_ao,
+                            p.n_nuc, p.size_bh, *_ptrs(mol), X.data_ptr())
+    torch.cuda.synchronize()
+    assert "n_slices" in cg.last_error()
+    assert (X.cpu().numpy() == 7.0).all()
 
 
 @pytest.mark.parametrize("rows", [None, 37])
