@@ -68,9 +68,10 @@ __global__ void expand_pairs_kernel(int64_t rows, int nA, const double *__restri
         return;
     const double *src = Xp + row * ldp;
     double *dst = X + row * nA2;
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nA2;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        const int a = (int)(k % nA), b = (int)(k / nA);
+    // nA^2 < 2^30 (the build's argument checks): 32-bit index arithmetic, one division
+    const int n2 = (int)nA2;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n2; k += gridDim.x * blockDim.x) {
+        const int b = k / nA, a = k - b * nA;
         dst[k] = src[a >= b ? tri_index(a, b, nA) : tri_index(b, a, nA)];
     }
 }
