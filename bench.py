@@ -719,6 +719,8 @@ def large_leg(cg, args, warmup, steps, with_accuracy, sizes=(3000, 6000), full_b
         # the whole r1 grid in one call: X (130 GB) is formed on the device in the
         # contractions' packed layout but not returned, int_2e (65 GB) stays on the device
         log("large: one full build, int_2e returned, X not copied out")
+        # the samples' workspace would otherwise shrink the free memory the build plans with
+        cg.load().cutc_release()
         dr = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in p.arrays().items()}
         torch.cuda.synchronize(dev)
         st = cg.Stats()
