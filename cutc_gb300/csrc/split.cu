@@ -289,7 +289,7 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                 fail(5);
         }
     } else {
-        // ---- epilogue: exact chunk flushes, then FP64 recombination ----------
+        // ---- epilogue: exact chunk flushes, then the error-free final sum ----
         const int q = warp & 3, cgrp = warp >> 2;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         const uint32_t coff = (uint32_t)(CW * cgrp);

@@ -35,7 +35,7 @@ extern "C" {
 
 /* ---- precision forms --------------------------------------------------- */
 #define CUTC_PLAIN_FP64 0 /* FP64 contractions: the drop-in form */
-#define CUTC_SPLIT_BF16 1 /* FP64 operands split into BF16 slices on tcgen05, FP64 recombination */
+#define CUTC_SPLIT_BF16 1 /* FP64 operands split into BF16 slices on tcgen05, exact FP32 sums, FP64 result */
 
 /*
  * Drop-in replacement for CuTC's cutc_int (src/cutc_int.c:15-20).
