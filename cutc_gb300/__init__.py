@@ -31,6 +31,7 @@ SPLIT_BF16 = 1
 # every symbol include/cutc_int.h declares
 EXPORTS = ["cutc_int", "cutc_int_ex", "cutc_int_scan", "cutc_default_options", "cutc_jast_bh_dev",
            "cutc_jast_bh_dev_noalloc", "cutc_split_gemm_dev", "cutc_fp64_gemm_dev",
+           "cutc_check_wait_limit",
            "cutc_validate_launch_dims",
            "cutc_last_error", "cutc_release", "cutc_server_default_config", "cutc_server_create",
            "cutc_server_submit", "cutc_server_wait", "cutc_server_get_stats", "cutc_server_destroy",
@@ -170,6 +171,8 @@ def load(path: str = LIB_PATH):
     L.cutc_last_error.restype = ctypes.c_char_p
     L.cutc_release.argtypes = []
     L.cutc_release.restype = None
+    L.cutc_check_wait_limit.argtypes = []
+    L.cutc_check_wait_limit.restype = i
     L.trans_inplace.argtypes = [vp, i]
     L.trans_inplace.restype = None
     L.trans_pqst_psqt_inplace.argtypes = [i, vp]

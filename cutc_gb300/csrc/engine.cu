@@ -1232,6 +1232,14 @@ extern "C" int cutc_int_scan(const cutc_options *opt, int n_sets, int n_grid1, i
     return CUTC_OK;
 }
 
+extern "C" int cutc_check_wait_limit(void)
+{
+    Engine *E = nullptr;
+    CUTC_TRY(get_engine(&E));
+    std::lock_guard<std::mutex> lk(E->mu);
+    return split_wait_limit_check(E);
+}
+
 extern "C" int cutc_jast_bh_dev(int i0, int n1b, int n_grid1, int n_grid2, int n_nuc, int size_bh,
                                 const double *r1, const double *r2, const double *rn,
                                 const double *c_bh, const int *m_bh, const int *n_bh,

@@ -1467,6 +1467,40 @@ int split_pair_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp,
                                : pair_tile<5>(E, st, sp, P, rn, a_en);
 }
 
+// One CTA waits on a pipeline barrier that nothing completes, with the bounded wait
+// the tensor-core kernels use; it records whether the wait gave up (2) or, against
+// all expectation, completed (1).
+__global__ void wait_limit_kernel(int *result)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(tc::smem_u32(&bar), 1);
+        tc::fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        *result = tc::mbar_wait(tc::smem_u32(&bar), 0, nullptr) ? 1 : 2;
+}
+
+int split_wait_limit_check(Engine *E)
+{
+    void *p;
+    CUTC_TRY(E->ws.get(240, 64, &p));
+    int *d = (int *)p;
+    CUTC_CUDA_TRY(cudaMemsetAsync(d, 0, 4, E->stream));
+    wait_limit_kernel<<<1, 32, 0, E->stream>>>(d);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    int h = 0;
+    CUTC_CUDA_TRY(cudaMemcpyAsync(&h, d, 4, cudaMemcpyDeviceToHost, E->stream));
+    CUTC_CUDA_TRY(cudaStreamSynchronize(E->stream));
+    if (h == 2) {
+        cutc_set_error(CUTC_ERR_TIMEOUT, "a pipeline wait gave up after its limit (as checked)");
+        return CUTC_ERR_TIMEOUT;
+    }
+    cutc_set_error(CUTC_ERR_CUDA, "the wait-limit check's barrier completed (result %d)", h);
+    return CUTC_ERR_CUDA;
+}
+
 int split_check(cudaStream_t st, SplitPlan &sp)
 {
     int herr = 0;

@@ -50,6 +50,9 @@ int split_k_blocks_per_launch(int64_t K, int64_t M, int k_split);
 size_t split_int2e_row_bytes(const Request &R);
 // Device bytes that do not depend on the tile size (the P slices).
 size_t split_fixed_bytes(const Request &R);
+// The bounded-wait check behind cutc_check_wait_limit: CUTC_ERR_TIMEOUT when the
+// wait gave up as designed.
+int split_wait_limit_check(Engine *E);
 int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *wr2,
                     const double *aos2v, int64_t n1t, int slot0, SplitPlan &sp);
 // X of one r1 tile from the df tile G[c][i][j] ((hi, lo) pairs), written into the

@@ -200,6 +200,15 @@ int cutc_jast_bh_dev_noalloc(int i0, int n1b, int n_grid1, int n_grid2, int n_nu
                              void *stream);
 
 /*
+ * The failure path of the tensor-core kernels' pipeline waits, checked without a
+ * fault: one CTA waits on a barrier that nothing completes, its bounded wait gives
+ * up after its limit (2 s), and the call returns CUTC_ERR_TIMEOUT -- the status a
+ * build reports when one of its pipeline waits gives up -- with the device still
+ * usable.  For tests.  No reference counterpart.
+ */
+int cutc_check_wait_limit(void);
+
+/*
  * The split-precision contraction alone, on device arrays of the current
  * device: C[m + ldc * n] = sum_k A[m * K + k] * B[n * K + k] for m < M, n < N,
  * with A and B FP64 row-major (K contiguous) and the product formed from
