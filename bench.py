@@ -14,10 +14,11 @@ sample of r1 rows, scaled to a full build.
 
 On one GPU the line also carries the rest of the metric, each measured in the
 same run: the error of both forms against the FP64 oracle (``accuracy``), the
-plain FP64 form's rate, the large workload on r1 samples (``large``), the
-Jastrow-parameter scan (``scan``), a prefix of the serving stream with p50/p99
-latency (``serving``) and the split contraction beside cuBLAS's own FP64
-emulation on the same operands (``rival``).
+plain FP64 form's rate, the split form at 6 slices (the plain form's error
+class, ``split_6_slices``), the large workload as one full build and on r1
+samples (``large``), the Jastrow-parameter scan (``scan``), a prefix of the
+serving stream with p50/p99 latency (``serving``) and the split contraction
+beside cuBLAS's own FP64 emulation on the same operands (``rival``).
 
 Under torchrun (N > 1) every rank runs an independent replica of the workload
 (the path is single-GPU; there is no collective on the data path) and the
