@@ -66,48 +66,6 @@ CUTC_HD long long scaled_round(double x, int e)
     return t;
 }
 
-// t for the exact sum x = hi + lo of a normalised double-float (|lo| <= ulp(hi)/2),
-// with no FP64 arithmetic: GB300 converts and adds FP64 at 1/64 of its FP32 rate,
-// which made the G slicer FP64-bound.  With V = |x| 2^(F - e) = A 2^-Q + B 2^-Q,
-// A = |hi| 2^(F - e + Q) an integer and B the signed part of lo,
-// floor(V 2^Q) = A + floor(B) and, as 2^(Q-1) is an integer,
-// floor(V + 1/2) = (floor(V 2^Q) + 2^(Q-1)) >> Q.
-template <int S>
-CUTC_HD long long scaled_round_df(float hi, float lo, int e)
-{
-    constexpr int F = 8 + 9 * (S - 1);
-    const unsigned hb = float_bits(hi), lb = float_bits(lo);
-    if ((hb & 0x7fffffffu) == 0u)
-        return 0;  // lo is zero too
-    const unsigned hexp = (hb >> 23) & 0xffu;
-    const unsigned long long mh = hexp ? ((hb & 0x7fffffu) | 0x800000u) : (hb & 0x7fffffu);
-    const int a = (hexp ? (int)hexp : 1) - 150 + F - e;  // |hi| 2^(F-e) = mh 2^a, a <= F - 23
-    const int Q = a < -1 ? -a : 1;
-    if (Q >= 26)
-        return 0;  // V < 2^(24 - Q) (1 + 2^-24) < 1/2
-    const unsigned long long A = mh << (a + Q);
-    long long fb = 0;
-    if ((lb & 0x7fffffffu) != 0u) {
-        const unsigned lexp = (lb >> 23) & 0xffu;
-        const unsigned long long ml = lexp ? ((lb & 0x7fffffu) | 0x800000u) : (lb & 0x7fffffu);
-        const int sh = (lexp ? (int)lexp : 1) - 150 + F - e + Q;  // |lo| 2^(F-e+Q) = ml 2^sh
-        const bool same = ((hb ^ lb) >> 31) == 0u;
-        if (sh >= 0) {  // not reached for a normalised pair (sh < 0)
-            const long long v = (long long)(ml << (sh < 39 ? sh : 39));
-            fb = same ? v : -v;
-        } else {
-            const int k = -sh;
-            if (same)
-                fb = k >= 64 ? 0 : (long long)(ml >> k);
-            else
-                fb = k >= 64 ? -1 : -(long long)((ml + (1ull << k) - 1) >> k);
-        }
-    }
-    const unsigned long long T = A + (unsigned long long)fb;  // the true sum is in [0, 2^64)
-    const long long r = (long long)((T + (1ull << (Q - 1))) >> Q);
-    return (hb >> 31) ? -r : r;
-}
-
 // IEEE FP32 operations, rounded to nearest, never contracted into FMAs (host builds of
 // this header take -ffp-contract=off)
 CUTC_HD float f_add(float a, float b)
@@ -151,7 +109,8 @@ CUTC_HD float pow2_float(int k)  // 2^k for k in [-126, 127]
 
 // The S digits of the normalised double-float hi + lo (|lo| <= ulp(hi)/2) of a row with
 // exponent e (|hi + lo| < 2^e), cut in FP32 arithmetic on the FMA pipe instead of the
-// 64-bit integer work of scaled_round_df + digits_int, which kept the integer pipe busy.
+// 64-bit integer work of an exact rounding followed by digits_int, which kept the
+// integer pipe busy.
 // With v = (hi + lo) 2^(8 - e) held as the pair (xh, xl), |v| < 256:
 //   q_s = rint(xh);  (xh, xl) <- TwoSum(xh - q_s, xl) * 2^9
 // (xh - q_s is exact, TwoSum is exact, the scaling is exact), so
