@@ -4,9 +4,9 @@
 // An operand value x of a row with exponent e (|x| < 2^e) is rounded at its
 // last digit, t = sign(x) floor(|x| 2^(F - e) + 1/2) with F = 8 + 9 (S - 1),
 // and t is cut into digits q_0 .. q_{S-1} (q_s in [-256, 255] for s > 0) with
-// t = sum_s q_s 2^(9 (S - 1 - s)).  Everything here is integer work, callable
-// from device code (the slicing kernels) and from host code, where a plain C++
-// build checks it against exact arithmetic.
+// t = sum_s q_s 2^(9 (S - 1 - s)).  Everything here is callable from device code
+// (the slicing kernels) and from host code, where a plain C++ build checks it
+// against exact arithmetic.
 #pragma once
 
 #include <stdint.h>
