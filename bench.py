@@ -500,7 +500,7 @@ def run_ours(args):
         executed = achieved * packed * n_products if n_products else None
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak, "traffic": traffic_per_launch(args, p, gemm_launches),
-                    "kernel": "split_gemm_kernel (X build, one launch per r1 tile)",
+                    "kernel": "split_gemm_kernel (X build: the K launches of each r1 tile)",
                     "peak_source": "bf16_tflops_sustained of %s" % peak_kind,
                     "alg_flops_per_launch": per_launch_flops, "ms_per_launch": per_launch_ms,
                     "executed_bf16_tflops": executed,
@@ -1148,11 +1148,12 @@ def traffic_per_launch(args, p, launches):
     try:
         with open(path) as f:
             d = json.load(f)
-        # bytes per (M x N x K) unit measured on the captured launch, scaled to this launch
+        # bytes per (M x N x K) unit measured on the captured launches, times the M N K
+        # of one launch: a build's X contractions (np x 4 n1 x n2) over its launches
         per_unit = float(d["dram_bytes_per_mnk"])
         np_ = p.n_ao * (p.n_ao + 1) // 2
-        n_per_launch = 4.0 * p.n_grid1 / max(1, launches / max(1, args.steps))
-        return per_unit * np_ * n_per_launch * p.n_grid2
+        launches_per_build = max(1.0, launches / max(1, args.steps))
+        return per_unit * np_ * 4.0 * p.n_grid1 * p.n_grid2 / launches_per_build
     except Exception:
         return None
 

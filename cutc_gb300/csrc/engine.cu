@@ -955,8 +955,15 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
             ms_i += ev_ms(e[4], e[5]);
             ms_tiles += ev_ms(e[0], e[5]);
         }
+        // a tile's X contraction is one FP64 launch, or the split form's K launches
+        int x_launches = 1;
+        if (R.precision == CUTC_SPLIT_BF16) {
+            const int64_t nkb = ((int64_t)R.n2 + 31) / 32;
+            const int64_t per = split_k_blocks_per_launch(nkb * 32, n_pairs(R.nA), R.k_split);
+            x_launches = (int)((nkb + per - 1) / per);
+        }
         stats->ms_x_gemm = ms_gemm;
-        stats->n_x_gemm = n_tiles;
+        stats->n_x_gemm = n_tiles * x_launches;
         stats->ms_h2d = ev_ms(E->ev[0], E->ev[1]);
         stats->ms_pair = ms_pair;
         stats->ms_x = ev_ms(E->ev[1], E->ev[2]) + ms_tiles - ms_pair - ms_i;

@@ -112,7 +112,8 @@ typedef struct cutc_stats {
     int n_r1_tiles;         /* r1 tiles the X build was split into */
     int gpu_launches;       /* kernels of this library launched by the call */
     double ms_x_gemm;       /* device time of the X-build contraction launches alone */
-    int n_x_gemm;           /* number of those launches (one per r1 tile) */
+    int n_x_gemm;           /* number of those launches: one per r1 tile (plain form),
+                               the K launches of each r1 tile (split form) */
 } cutc_stats;
 
 /* Fills the defaults: plain FP64, 5 slices, a_en = a_ee = 1, 3 X components. */

@@ -51,6 +51,25 @@ def test_split_r1_tiling_is_exact():
     assert oracle.rel_err(I2, I1)["max"] < 1e-12
 
 
+def test_split_k_launches():
+    """k_split cuts each contraction into K launches whose results are summed in FP64
+    (the path every X contraction longer than K = 65536 takes): the oracle's results at
+    the split tolerance, the one-launch build's within 1e-12, and the stats count every
+    X-contraction launch."""
+    p = synth.make_problem(n_nuc=3, n_ao=10, n_grid1=260, n_grid2=1500, size_bh=6, seed=31)
+    X1, I1, st1 = cg.build_integrals(p, cg.SPLIT_BF16, with_stats=True)
+    X2, I2, st2 = cg.build_integrals(p, cg.SPLIT_BF16, k_split=256, with_stats=True)
+    Xo, Io = oracle.cutc_int(p)
+    _check(X2, I2, Xo, Io)
+    assert oracle.rel_err(X2, X1)["max"] < 1e-12
+    assert oracle.rel_err(I2, I1)["max"] < 1e-12
+    # K = 1500 padded to 1504: 47 blocks of 32, 8 per launch
+    assert st1["n_x_gemm"] == st1["n_r1_tiles"]
+    assert st2["n_x_gemm"] == 6 * st2["n_r1_tiles"]
+    info = cg.plan(p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, cg.SPLIT_BF16, 5, k_split=256)
+    assert info["x_launches_per_tile"] == 6
+
+
 def test_split_four_components_and_scale_factors():
     p = synth.make_problem(n_nuc=2, n_ao=7, n_grid1=150, n_grid2=500, size_bh=5, seed=9,
                            a_en=1.3, a_ee=0.6)
