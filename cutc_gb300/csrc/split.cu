@@ -816,41 +816,80 @@ struct SrcDenseDF {  // hi + lo of X[r * ld + k]; the slicer reads the pair itse
     }
 };
 
-struct SrcSym {  // w[k] chi_a(k) chi_b(k), (a, b) = pairs[r]
+// The pair products take their first factor w chi_a from a table of the weighted AO
+// rows, formed once per AO (weighted_aos_kernel) instead of once per pair: FP64
+// multiplies run at 1/64 of the FP32 rate on GB300, and these sources are evaluated
+// twice per element (row maxima, then digits).
+struct SrcSym {  // w[k] chi_a(k) chi_b(k) = (w chi_a)(k) chi_b(k), (a, b) = pairs[r]
     static constexpr bool kDoubleFloat = false;
-    const double *w, *chi;
-    int64_t ldchi;
+    const double *wchi, *chi;  // wchi[a * K + k] = w[k] chi_a(k); chi_b at chi[b * ldchi + k]
+    int64_t K, ldchi;
     const int2 *pairs;
     __device__ double operator()(int64_t r, int64_t k) const
     {
         const int2 ab = pairs[r];
-        const double wa = w[k] * chi[ab.x * ldchi + k];
-        return wa * chi[ab.y * ldchi + k];
+        return wchi[ab.x * K + k] * chi[ab.y * ldchi + k];
     }
 };
 
-struct SrcAnti {  // w (chi_c d_m chi_d - chi_d d_m chi_c), k = m n + g, (c, d) = pairs[r]
+// w (chi_c d_m chi_d - chi_d d_m chi_c) as (w chi_c) d_m chi_d - (w chi_d) d_m chi_c,
+// k = m n + g, (c, d) = pairs[r]
+struct SrcAnti {
     static constexpr bool kDoubleFloat = false;
-    const double *w, *aos;  // aos: (ld, nA, 4) with the grid offset already applied
-    int n, nA;              // n: grid points counted in k (g < n)
-    int64_t ld;             // grid stride of aos
+    const double *wchi, *aos;  // wchi[c * n + g] = w[g] chi_c(g); aos: (ld, nA, 4) with
+                               // the grid offset already applied
+    int n, nA;                 // n: grid points counted in k (g < n)
+    int64_t ld;                // grid stride of aos
     const int2 *pairs;
     __device__ double operator()(int64_t r, int64_t k) const
     {
-        const int m = (int)(k / n), g = (int)(k % n);
+        int m, g;
+        if (k < 0x7fffffff) {  // 32-bit division (K = 3 n)
+            const unsigned ku = (unsigned)k, mu = ku / (unsigned)n;
+            m = (int)mu;
+            g = (int)(ku - mu * (unsigned)n);
+        } else {
+            m = (int)(k / n);
+            g = (int)(k % n);
+        }
         const int2 cd = pairs[r];
         const int64_t comp = (int64_t)nA * ld * (m + 1);
-        const double vc = aos[cd.x * ld + g], vd = aos[cd.y * ld + g];
-        return w[g] * (vc * aos[comp + cd.y * ld + g] - vd * aos[comp + cd.x * ld + g]);
+        return fma(wchi[(int64_t)cd.x * n + g], aos[comp + cd.y * ld + g],
+                   -(wchi[(int64_t)cd.y * n + g] * aos[comp + cd.x * ld + g]));
     }
 };
 
-__device__ __forceinline__ void atomic_max_abs(unsigned long long *dst, double v)
+// wchi[a * n + g] = w[g] chi_a(g), chi_a at chi[a * ldchi]
+__global__ void weighted_aos_kernel(int n, const double *__restrict__ w,
+                                    const double *__restrict__ chi, int64_t ldchi,
+                                    double *__restrict__ wchi)
 {
-    atomicMax(dst, (unsigned long long)__double_as_longlong(fabs(v)));
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = blockIdx.y;
+    if (g < n)
+        wchi[(int64_t)a * n + g] = w[g] * chi[(int64_t)a * ldchi + g];
 }
 
-// rmax[r] = bits of max_k |src(r, k)| (non-negative doubles order like their bits)
+static int weighted_aos(cudaStream_t st, int n, int nA, const double *w, const double *chi,
+                        int64_t ldchi, double *wchi)
+{
+    if (n <= 0 || nA <= 0)
+        return CUTC_OK;
+    weighted_aos_kernel<<<dim3(ceil_div(n, 256), nA), 256, 0, st>>>(n, w, chi, ldchi, wchi);
+    CUTC_CUDA_TRY(cudaGetLastError());
+    note_launches(1);
+    return CUTC_OK;
+}
+
+// |v| as its bits (non-negative doubles order like their bits); NaN counts as 0, as
+// fmax would skip it.  Integer work: an FP64 max would take the FP64 pipe.
+__device__ __forceinline__ unsigned long long abs_bits(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    return b > 0x7ff0000000000000ull ? 0ull : b;
+}
+
+// rmax[r] = bits of max_k |src(r, k)|
 template <class Src>
 __global__ void rowmax_kernel(Src src, int rows, int64_t K, int64_t kper,
                               unsigned long long *rmax)
@@ -860,23 +899,29 @@ __global__ void rowmax_kernel(Src src, int rows, int64_t K, int64_t kper,
         return;
     const int64_t k0 = (int64_t)blockIdx.y * kper;
     const int64_t k1 = min(K, k0 + kper);
-    double m = 0.0;
-    for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x)
-        m = fmax(m, fabs(src(r, k)));
+    unsigned long long m = 0;
+    for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+        const unsigned long long b = abs_bits(src(r, k));
+        m = b > m ? b : m;
+    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long b = __shfl_xor_sync(0xffffffffu, m, o);
+        m = b > m ? b : m;
+    }
+    __shared__ unsigned long long red[32];
     if ((threadIdx.x & 31) == 0)
         red[threadIdx.x >> 5] = m;
     __syncthreads();
     if (threadIdx.x < 32) {
-        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0ull;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (threadIdx.x == 0 && m > 0.0)
-            atomic_max_abs(&rmax[r], m);
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long b = __shfl_xor_sync(0xffffffffu, m, o);
+            m = b > m ? b : m;
+        }
+        if (threadIdx.x == 0 && m > 0)
+            atomicMax(&rmax[r], m);
     }
 }
 
@@ -888,11 +933,13 @@ __global__ void rowmax_cols_kernel(const double *X, int64_t ld, int64_t k0, int 
     if (r >= rows)
         return;
     const int64_t ka = (int64_t)blockIdx.y * kper, kb = min(K, ka + kper);
-    double m = 0.0;
-    for (int64_t k = ka; k < kb; k++)
-        m = fmax(m, fabs(X[(k0 + k) * ld + r]));
-    if (m > 0.0)
-        atomic_max_abs(&rmax[r], m);
+    unsigned long long m = 0;
+    for (int64_t k = ka; k < kb; k++) {
+        const unsigned long long b = abs_bits(X[(k0 + k) * ld + r]);
+        m = b > m ? b : m;
+    }
+    if (m > 0)
+        atomicMax(&rmax[r], m);
 }
 
 // Exponent e with |x| < 2^e for every x of the row; 0 for zero (or denormal-only) rows.
@@ -1185,6 +1232,7 @@ enum SplitSlot {
     SS_PAIRS_SYM = 0, SS_PAIRS_ANTI = 1, SS_ERR = 2,
     SS_AX = 3, SS_BX = 6, SS_AH = 9, SS_AN = 12, SS_BH = 15, SS_BN = 18,
     SS_AF = 21, SS_BC = 24, SS_F64 = 27, SS_C64 = 28, SS_R1D = 29, SS_BSCALE = 30,
+    SS_WCHI2 = 31, SS_WCHI1 = 32,
 };
 
 
@@ -1198,14 +1246,17 @@ size_t split_int2e_row_bytes(const Request &R)
 {
     const int64_t np = n_pairs(R.nA), nl = std::max<int64_t>(1, n_strict_pairs(R.nA));
     const int bn = bn_for(R.n_slices);
-    // the point's K columns of the int_2e operands (X_3, X_012, S0, S)
+    // the point's K columns of the int_2e operands (X_3, X_012, S0, S), and its
+    // weighted AO values w chi_a
     return 2 * (size_t)R.n_slices * (round_up(np, kBM) * 4 + round_up(np, bn) +
-                                     3 * (size_t)round_up(nl, bn)) + 64;
+                                     3 * (size_t)round_up(nl, bn)) + 8 * (size_t)R.nA + 64;
 }
 
 size_t split_fixed_bytes(const Request &R)
 {
-    return 2 * (size_t)R.n_slices * round_up(n_pairs(R.nA), kBM) * round_up(R.n2, kBK);
+    // P slices and the weighted AO values w chi_a on r2 they are formed from
+    return 2 * (size_t)R.n_slices * round_up(n_pairs(R.nA), kBM) * round_up(R.n2, kBK) +
+           8 * (size_t)R.nA * R.n2;
 }
 
 static int upload_pairs(Workspace &W, int slot, cudaStream_t st, int nA, bool strict, int2 **out)
@@ -1253,9 +1304,12 @@ int split_prepare_x(Engine *E, const Request &R, cudaStream_t st, const double *
     CUTC_TRY(alloc_operand(W, slot0 + SS_AX, R.n_slices, np, kBM, R.n2, S_.AX));
     CUTC_TRY(alloc_operand(W, slot0 + SS_BX, R.n_slices, (int)(4 * n1t), bn_for(R.n_slices), R.n2,
                            S_.BX));
-    SrcSym src{wr2, aos2v, (int64_t)R.n2, S_.pairs_sym};
     if (R.mol_tag && E->tag_x == R.mol_tag && E->tag_x_buf == S_.AX.sl)
         return CUTC_OK;  // the same molecule's P slices are already there
+    CUTC_TRY(W.get(slot0 + SS_WCHI2, std::max<size_t>(1, (size_t)R.nA * R.n2) * 8, &p));
+    double *wchi = (double *)p;
+    CUTC_TRY(weighted_aos(st, R.n2, R.nA, wr2, aos2v, (int64_t)R.n2, wchi));
+    SrcSym src{wchi, aos2v, (int64_t)R.n2, (int64_t)R.n2, S_.pairs_sym};
     CUTC_SLICES_DISPATCH(R.n_slices, CUTC_TRY((slice_rows<S, SrcSym>(st, src, S_.AX))));
     E->tag_x = R.mol_tag;
     E->tag_x_buf = S_.AX.sl;
@@ -1301,12 +1355,17 @@ int split_int2e_tile(Engine *E, const Request &R, cudaStream_t st, SplitPlan &sp
     CUTC_TRY(alloc_operand(W, slot0 + SS_BH, sp.n_slices, np, bn, nb, BH));
     CUTC_TRY(alloc_operand(W, slot0 + SS_BN, sp.n_slices, std::max(nl, 1), bn, 3 * (int64_t)nb, BN));
     BN.M = nl;
-    SrcSym s0{wr1, aos1, ld1, S_.pairs_sym};
-    SrcAnti sa{wr1, aos1, nb, nA, ld1, S_.pairs_anti};
     const int acc = first ? 0 : 1;
     // With the whole r1 grid in one tile the B operands depend on the molecule
     // only, and a build with the same molecule tag keeps them.
     const bool keep_b = nb == R.n1 && R.mol_tag && E->tag_i == R.mol_tag && E->tag_i_buf == BH.sl;
+    void *p;
+    CUTC_TRY(W.get(slot0 + SS_WCHI1, std::max<size_t>(1, (size_t)nA * nb) * 8, &p));
+    double *wchi = (double *)p;
+    if (!keep_b)
+        CUTC_TRY(weighted_aos(st, nb, nA, wr1, aos1, ld1, wchi));
+    SrcSym s0{wchi, aos1, (int64_t)nb, ld1, S_.pairs_sym};
+    SrcAnti sa{wchi, aos1, nb, nA, ld1, S_.pairs_anti};
     CUTC_SLICES_DISPATCH(sp.n_slices, {
         // Xt[(m nb + i) np + p]: X_3 is column block 3, X_012 the blocks 0..2
         CUTC_TRY(slice_cols<S>(st, Xt, np, 3 * (int64_t)nb, AH));
