@@ -813,6 +813,27 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
                                   !R.pair_fp64));
         }
 
+        // the tile's X rows in the reference layout X[m][i][b][a], before the int_2e share,
+        // so that their copy to the host overlaps the int_2e contractions
+        if (R.i_only) {
+            // X stays packed in the int_2e block and is not returned
+        } else if (out_dev) {
+            for (int m = 0; m < R.x_components; m++)
+                CUTC_TRY(launch_expand_pairs(st, nb, nA, d_Xt + ((int64_t)m * blk_rows + ib) * np,
+                                             np, R.X + ((int64_t)m * n1 + i0) * nA2));
+        } else {
+            const int b = tile & 1;
+            if (busy[b])
+                CUTC_CUDA_TRY(cudaStreamWaitEvent(st, done[b], 0));
+            for (int m = 0; m < R.x_components; m++)
+                CUTC_TRY(launch_expand_pairs(st, nb, nA, d_Xt + ((int64_t)m * blk_rows + ib) * np,
+                                             np, stage_x[b] + (int64_t)m * nb * nA2));
+            CUTC_CUDA_TRY(cudaEventRecord(ready[b], st));
+            CUTC_TRY(copy_x(tile));
+        }
+        if (!R.i_only)
+            note_launches(R.x_components);
+
         // the block's share of int_2e once its last tile is in
         // (src/build_int_2e_ao.cu:60-67 and 97-104, packed):
         //   H += X_3 S0,   N += -1/2 [X_0 X_1 X_2] S   over the block's r1 points
@@ -849,28 +870,9 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         }
         if (tev)
             CUTC_CUDA_TRY(cudaEventRecord(tev[5], st));
-
-        // the tile's X rows in the reference layout X[m][i][b][a]
-        if (R.i_only) {
-            // X stays packed in the int_2e block and is not returned
-        } else if (out_dev) {
-            for (int m = 0; m < R.x_components; m++)
-                CUTC_TRY(launch_expand_pairs(st, nb, nA, d_Xt + ((int64_t)m * blk_rows + ib) * np,
-                                             np, R.X + ((int64_t)m * n1 + i0) * nA2));
-        } else {
-            const int b = tile & 1;
-            if (busy[b])
-                CUTC_CUDA_TRY(cudaStreamWaitEvent(st, done[b], 0));
-            for (int m = 0; m < R.x_components; m++)
-                CUTC_TRY(launch_expand_pairs(st, nb, nA, d_Xt + ((int64_t)m * blk_rows + ib) * np,
-                                             np, stage_x[b] + (int64_t)m * nb * nA2));
-            CUTC_CUDA_TRY(cudaEventRecord(ready[b], st));
-            CUTC_TRY(copy_x(tile));
-            if (tile > 0)
-                CUTC_TRY(finish_x(tile - 1));
-        }
-        if (!R.i_only)
-            note_launches(R.x_components);
+        // the previous tile's rows, pinned -> pageable, while the device works on this one
+        if (!out_dev && !R.i_only && tile > 0)
+            CUTC_TRY(finish_x(tile - 1));
         if (i0 + nb == blk0 + blk_rows) {  // next block
             blk0 += blk_rows;
             blk_rows = (int)std::min<int64_t>(kb, n1 - blk0);
