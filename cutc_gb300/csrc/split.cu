@@ -86,7 +86,7 @@ constexpr int kBigM = 16384;
 constexpr int kLongKBigM = 32768;
 constexpr int kLaunchKBigM = 24576;
 constexpr uint32_t kTmemCols = 512;
-constexpr int kGroupM = 8;      // row tiles per raster group (A tiles shared through L2)
+constexpr int kGroupN = 8;      // column tiles per raster group (B tiles shared through L2)
 
 // Output-column tile for S slices: S diagonals x 2 buffers must fit 512 columns
 // and the widest instruction (N = BN S) must not exceed 256.
@@ -171,14 +171,16 @@ split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     volatile int *s_abort = reinterpret_cast<volatile int *>(s_tmem + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // grouped raster: kGroupM row tiles share the A tiles through L2
+    // grouped raster: a group of kGroupN column tiles sweeps the row tiles, so the
+    // CTAs of a wave share their B tiles and a few A tiles through L2 (0.4-1% faster
+    // than groups of 8 row tiles sweeping the columns, on the large and medium X builds)
     const int num_m = P.Mpad / kBM, num_n = P.Npad / BN;
-    const int per_group = kGroupM * num_n;
     const int tid = blockIdx.x;
-    const int gfirst = (tid / per_group) * kGroupM;
-    const int gsize = min(num_m - gfirst, kGroupM);
-    const int m0 = (gfirst + (tid % per_group) % gsize) * kBM;
-    const int n0 = ((tid % per_group) / gsize) * BN;
+    const int per_group = kGroupN * num_m;
+    const int gfirst = (tid / per_group) * kGroupN;
+    const int gsize = min(num_n - gfirst, kGroupN);
+    const int n0 = (gfirst + (tid % per_group) % gsize) * BN;
+    const int m0 = ((tid % per_group) / gsize) * kBM;
     const int nkb = P.nkb;
     const int nch = (nkb + kChunkBlocks - 1) / kChunkBlocks;
 
