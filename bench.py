@@ -25,7 +25,7 @@ Under torchrun (N > 1) every rank runs an independent replica of the workload
 reported value is the sum over ranks: weak scaling.
 
 Micro-benchmarks of single kernels (the cases the committed ncu summaries were
-captured on): ``--kernel split_gemm|fp64_gemm|pair|plain_build|rival``.
+captured on) and device-resident sample builds: ``--kernel split_gemm|fp64_gemm|pair|plain_build|sample_build|rival``.
 """
 from __future__ import annotations
 
@@ -1214,6 +1214,24 @@ def run_kernel(args):
                           "ms_x_gemm": st["ms_x_gemm"], "ms_int2e": st["ms_int2e"],
                           "ms_pair": st["ms_pair"],
                           "x_gemm_fp64_tflops": flops_x / st["ms_x_gemm"] / 1e9}))
+    elif k == "sample_build":
+        # device-resident builds of `rows` r1 points spread over the grid of --config (the
+        # whole grid when rows >= n_grid1), outputs on the device, per-build phase times
+        p = synth.make_config(args.config)
+        sub = synth.r1_sample(p, args.rows) if args.rows < p.n_grid1 else p
+        prec = cg.SPLIT_BF16 if args.precision == "split" else cg.PLAIN_FP64
+        dev = torch.device("cuda", 0)
+        nA2 = p.n_ao ** 2
+        out = (torch.empty((3, sub.n_grid1, nA2), dtype=torch.float64, device=dev),
+               torch.empty((nA2, nA2), dtype=torch.float64, device=dev))
+        runs = []
+        for _ in range(args.reps):
+            _, _, st = cg.build_integrals_device(sub, prec, n_slices=args.slices, out=out,
+                                                 with_stats=True)
+            runs.append({key: st[key] for key in ("ms_total", "ms_x_gemm", "n_x_gemm",
+                                                  "n_r1_tiles", "ms_pair", "ms_int2e")})
+        print(json.dumps({"kernel": k, "config": args.config, "rows": sub.n_grid1,
+                          "precision": args.precision, "builds": runs}))
     elif k == "rival":
         p = synth.make_config("medium")
         dev = torch.device("cuda", 0)
@@ -1317,7 +1335,8 @@ def main(argv=None):
     ap.add_argument("--scan-batch", type=int, default=8)
     ap.add_argument("--r1-sample", type=int, default=6000,
                     help="large workload: r1 rows of the bigger of the two timed samples")
-    ap.add_argument("--kernel", choices=["split_gemm", "fp64_gemm", "pair", "plain_build", "rival"],
+    ap.add_argument("--kernel", choices=["split_gemm", "fp64_gemm", "pair", "plain_build",
+                                         "sample_build", "rival"],
                     help="run one kernel's micro-benchmark instead")
     ap.add_argument("--m", type=int, default=7260)
     ap.add_argument("--n", type=int, default=2048)
