@@ -68,6 +68,8 @@ int Workspace::get(int slot, size_t bytes, void **out)
     if (b.cap < bytes) {
         if (b.p) {
             cudaFree(b.p);
+            if (slot >= kFirstReusableSlot)
+                reusable -= b.cap;
             b.p = nullptr;
             b.cap = 0;
         }
@@ -79,6 +81,8 @@ int Workspace::get(int slot, size_t bytes, void **out)
             return CUTC_ERR_NO_MEMORY;
         }
         b.cap = bytes;
+        if (slot >= kFirstReusableSlot)
+            reusable += bytes;
     }
     *out = b.p;
     return CUTC_OK;
@@ -162,10 +166,24 @@ void Workspace::release()
         if (b.p)
             cudaFree(b.p);
     bufs.clear();
+    reusable = 0;
 }
 
 static std::mutex g_engines_mu;
 static std::vector<Engine *> g_engines;
+
+// Working-buffer bytes held by the current device's engine (0 without one): the default
+// budget counts them as available.
+static size_t engine_reusable_bytes()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    std::lock_guard<std::mutex> lk(g_engines_mu);
+    return dev < (int)g_engines.size() && g_engines[dev] ? g_engines[dev]->ws.reusable.load() : 0;
+}
 
 int make_engine(int dev, Engine **out)
 {
@@ -348,6 +366,8 @@ enum Slot {
     S_R2D, S_F2D, S_POLY, S_BASIS,
     S_SPLIT0  // split-form slots follow
 };
+// the inputs of the build in progress come before the working buffers
+static_assert(S_T1 == kFirstReusableSlot, "input slots precede the reusable working buffers");
 
 static inline double ev_ms(cudaEvent_t a, cudaEvent_t b)
 {
@@ -588,6 +608,7 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     if (budget == 0) {
         size_t free_b = 0, total_b = 0;
         CUTC_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+        free_b += E->ws.reusable.load();  // this engine's working buffers are reused
         budget = std::min<size_t>((size_t)24 << 30, free_b / 4);
         const size_t fixed = fixed_bytes(R);
         if (free_b > fixed)
@@ -1389,6 +1410,7 @@ extern "C" int cutc_plan(const cutc_options *opt, int n_grid1, int n_grid2, int 
                            cudaGetErrorString(e));
             return CUTC_ERR_NO_DEVICE;
         }
+        free_b += engine_reusable_bytes();  // as a build on this device's engine counts them
         budget = std::min<size_t>((size_t)24 << 30, free_b / 4);
         const size_t fixed = fixed_bytes(R);
         if (free_b > fixed)

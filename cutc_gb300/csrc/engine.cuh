@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -24,13 +25,19 @@ struct PinnedPool {
     void release();
 };
 
-// Grow-only device buffers, one per slot, reused across calls.
+// Grow-only device buffers, one per slot, reused across calls.  Slots from
+// kFirstReusableSlot on hold a build's working buffers (tiles, blocks, operands), which
+// the next build reuses or frees and regrows: the default budget counts their bytes
+// (`reusable`, readable from any thread) as available beside the device's free memory,
+// so a build planned next to a previous build's buffers gets the same plan as a lone build.
+constexpr int kFirstReusableSlot = 10;
 struct Workspace {
     struct Buf {
         void *p = nullptr;
         size_t cap = 0;
     };
     std::vector<Buf> bufs;
+    std::atomic<size_t> reusable{0};
     int get(int slot, size_t bytes, void **out);
     void release();
 };
