@@ -68,8 +68,6 @@ int Workspace::get(int slot, size_t bytes, void **out)
     if (b.cap < bytes) {
         if (b.p) {
             cudaFree(b.p);
-            if (slot >= kFirstReusableSlot)
-                reusable -= b.cap;
             b.p = nullptr;
             b.cap = 0;
         }
@@ -81,8 +79,6 @@ int Workspace::get(int slot, size_t bytes, void **out)
             return CUTC_ERR_NO_MEMORY;
         }
         b.cap = bytes;
-        if (slot >= kFirstReusableSlot)
-            reusable += bytes;
     }
     *out = b.p;
     return CUTC_OK;
@@ -166,23 +162,39 @@ void Workspace::release()
         if (b.p)
             cudaFree(b.p);
     bufs.clear();
-    reusable = 0;
+    std::lock_guard<std::mutex> lk(memo_mu);
+    memo = PlanMemo{};
+}
+
+bool Workspace::recall(uint64_t key, PlanMemo *out)
+{
+    std::lock_guard<std::mutex> lk(memo_mu);
+    if (memo.key == 0 || memo.key != key)
+        return false;
+    *out = memo;
+    return true;
+}
+
+void Workspace::remember(const PlanMemo &m)
+{
+    std::lock_guard<std::mutex> lk(memo_mu);
+    memo = m;
 }
 
 static std::mutex g_engines_mu;
 static std::vector<Engine *> g_engines;
 
-// Working-buffer bytes held by the current device's engine (0 without one): the default
-// budget counts them as available.
-static size_t engine_reusable_bytes()
+// The remembered default plan of the current device's engine for a build of shape
+// `key` (false without an engine or a plan of that shape).
+static bool engine_recall(uint64_t key, PlanMemo *out)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
-        return 0;
+        return false;
     }
     std::lock_guard<std::mutex> lk(g_engines_mu);
-    return dev < (int)g_engines.size() && g_engines[dev] ? g_engines[dev]->ws.reusable.load() : 0;
+    return dev < (int)g_engines.size() && g_engines[dev] && g_engines[dev]->ws.recall(key, out);
 }
 
 int make_engine(int dev, Engine **out)
@@ -366,8 +378,6 @@ enum Slot {
     S_R2D, S_F2D, S_POLY, S_BASIS,
     S_SPLIT0  // split-form slots follow
 };
-// the inputs of the build in progress come before the working buffers
-static_assert(S_T1 == kFirstReusableSlot, "input slots precede the reusable working buffers");
 
 static inline double ev_ms(cudaEvent_t a, cudaEvent_t b)
 {
@@ -435,6 +445,22 @@ static size_t int2e_row_bytes(const Request &R)
     else
         b += split_int2e_row_bytes(R);
     return b;
+}
+
+// The shape of a build as far as the sizes of its working buffers go (FNV-1a over the
+// fields that set them; never 0).
+static uint64_t plan_key(const Request &R)
+{
+    const int64_t f[] = {R.n1, R.n2, R.nA, R.nN, R.precision, R.n_slices, R.x_components,
+                         (R.device_pointers || R.out_device) ? 1 : 0, R.x_only, R.i_only,
+                         R.tile_rows, R.int2e_rows};
+    uint64_t h = 1469598103934665603ull;
+    for (int64_t v : f)
+        for (int k = 0; k < 8; k++) {
+            h ^= (uint64_t)(v >> (8 * k)) & 0xffu;
+            h *= 1099511628211ull;
+        }
+    return h ? h : 1;
 }
 
 // r1 rows per X tile and per int_2e block for a budget (each gets the budget): the
@@ -605,17 +631,31 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
     // and N in FP64.  Device memory is the fixed part plus one tile and one block,
     // each within the budget.
     size_t budget = R.max_work_bytes;
-    if (budget == 0) {
-        size_t free_b = 0, total_b = 0;
-        CUTC_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
-        free_b += E->ws.reusable.load();  // this engine's working buffers are reused
-        budget = std::min<size_t>((size_t)24 << 30, free_b / 4);
-        const size_t fixed = fixed_bytes(R);
-        if (free_b > fixed)
-            budget = std::min<size_t>(budget, (size_t)((double)(free_b - fixed) * 0.4));
-    }
     int64_t n1t, kb;
-    plan_rows(R, budget, &n1t, &kb);
+    PlanMemo memo;
+    const uint64_t key = plan_key(R);
+    // which pair-term buffers the build holds besides: the remembered plan is taken
+    // only when they are the same
+    uint64_t path = 1 + (R.pair_fp64 ? 2 : 0);
+    if (R.precision == CUTC_SPLIT_BF16 && !R.pair_fp64)
+        path += 4 * (uint64_t)split_pair_tc_ok(R, exps.data(), nt) +
+                8 * (uint64_t)pair_df_max_exp(exps.data(), nt);
+    const bool default_budget = budget == 0;
+    if (default_budget && E->ws.recall(key, &memo) && memo.path == path) {
+        budget = memo.budget;  // the last build of this shape: its buffers fit this plan
+        n1t = memo.n1t;
+        kb = memo.kb;
+    } else {
+        if (default_budget) {
+            size_t free_b = 0, total_b = 0;
+            CUTC_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+            budget = std::min<size_t>((size_t)24 << 30, free_b / 4);
+            const size_t fixed = fixed_bytes(R);
+            if (free_b > fixed)
+                budget = std::min<size_t>(budget, (size_t)((double)(free_b - fixed) * 0.4));
+        }
+        plan_rows(R, budget, &n1t, &kb);
+    }
     const int n_tiles = (int)((n1 + n1t - 1) / n1t);
     constexpr int kTileEv = 6;
     if (stats) {
@@ -995,6 +1035,14 @@ int run_build(Engine *E, const Request &R_in, cutc_stats *stats)
         stats->ms_total = ev_ms(E->ev[0], E->ev[8]);
         stats->n_r1_tiles = n_tiles;
         stats->gpu_launches = (int)(launches_so_far() - launches0);
+    }
+    if (default_budget) {  // completed: the buffers of this shape hold this plan
+        memo.key = key;
+        memo.path = path;
+        memo.budget = budget;
+        memo.n1t = n1t;
+        memo.kb = kb;
+        E->ws.remember(memo);
     }
     return CUTC_OK;
 }
@@ -1401,23 +1449,29 @@ extern "C" int cutc_plan(const cutc_options *opt, int n_grid1, int n_grid2, int 
     if (const char *ir = getenv("CUTC_INT2E_ROWS"))
         R.int2e_rows = atoi(ir);
     size_t budget = opt->max_work_bytes;
-    if (budget == 0) {
-        size_t free_b = 0, total_b = 0;
-        cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            cutc_set_error(CUTC_ERR_NO_DEVICE, "no device to size the default budget: %s",
-                           cudaGetErrorString(e));
-            return CUTC_ERR_NO_DEVICE;
-        }
-        free_b += engine_reusable_bytes();  // as a build on this device's engine counts them
-        budget = std::min<size_t>((size_t)24 << 30, free_b / 4);
-        const size_t fixed = fixed_bytes(R);
-        if (free_b > fixed)
-            budget = std::min<size_t>(budget, (size_t)((double)(free_b - fixed) * 0.4));
-    }
     int64_t n1t, kb;
-    plan_rows(R, budget, &n1t, &kb);
+    PlanMemo memo;
+    if (budget == 0 && engine_recall(plan_key(R), &memo)) {
+        budget = memo.budget;  // as a build of this shape on the device's engine would
+        n1t = memo.n1t;
+        kb = memo.kb;
+    } else {
+        if (budget == 0) {
+            size_t free_b = 0, total_b = 0;
+            cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                cutc_set_error(CUTC_ERR_NO_DEVICE, "no device to size the default budget: %s",
+                               cudaGetErrorString(e));
+                return CUTC_ERR_NO_DEVICE;
+            }
+            budget = std::min<size_t>((size_t)24 << 30, free_b / 4);
+            const size_t fixed = fixed_bytes(R);
+            if (free_b > fixed)
+                budget = std::min<size_t>(budget, (size_t)((double)(free_b - fixed) * 0.4));
+        }
+        plan_rows(R, budget, &n1t, &kb);
+    }
     plan->tile_rows = (int)n1t;
     plan->block_rows = (int)kb;
     plan->n_tiles = (int)((n_grid1 + n1t - 1) / n1t);

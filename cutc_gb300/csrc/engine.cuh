@@ -25,21 +25,36 @@ struct PinnedPool {
     void release();
 };
 
-// Grow-only device buffers, one per slot, reused across calls.  Slots from
-// kFirstReusableSlot on hold a build's working buffers (tiles, blocks, operands), which
-// the next build reuses or frees and regrows: the default budget counts their bytes
-// (`reusable`, readable from any thread) as available beside the device's free memory,
-// so a build planned next to a previous build's buffers gets the same plan as a lone build.
-constexpr int kFirstReusableSlot = 10;
+// Grow-only device buffers, one per slot, reused across calls.
+//
+// The default plan of a build (r1 rows per tile and per int_2e block) is sized from the
+// device's free memory, which the buffers kept from the previous build no longer count
+// in.  So the workspace remembers the plan of its last completed default-budget build
+// with its shape (the fields that set the buffer sizes): a build of the same shape takes
+// that plan again, reusing every buffer at its size.  Repeated builds of a molecule then
+// tile r1 alike (same bits in the split form, whose int_2e row scales are per block)
+// however much memory the first build left held.
+struct PlanMemo {
+    uint64_t key = 0;   // 0: none
+    uint64_t path = 0;  // the pair-term path of that build (its other buffers)
+    size_t budget = 0;
+    int64_t n1t = 0, kb = 0;
+};
 struct Workspace {
     struct Buf {
         void *p = nullptr;
         size_t cap = 0;
     };
     std::vector<Buf> bufs;
-    std::atomic<size_t> reusable{0};
     int get(int slot, size_t bytes, void **out);
     void release();
+    // the remembered plan (readable from any thread)
+    bool recall(uint64_t key, PlanMemo *out);
+    void remember(const PlanMemo &m);
+
+  private:
+    std::mutex memo_mu;
+    PlanMemo memo;
 };
 
 struct Engine {

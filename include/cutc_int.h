@@ -304,8 +304,8 @@ int cutc_unpin_host(void *ptr);
 
 /* The device-memory plan of a build, computed on the host (no GPU needed when
  * opt->max_work_bytes is set; with 0 the budget follows the current device's
- * free memory plus the working buffers its engine keeps from the previous
- * build, as a build would).  The r1 grid is cut into X tiles of
+ * free memory, or is the plan of the engine's last completed build of the same
+ * shape, as a build would take it).  The r1 grid is cut into X tiles of
  * tile_rows points; the int_2e contractions run once per block of block_rows
  * points (whole tiles).  Device bytes besides the caller's arrays: fixed_bytes
  * + tile_rows * tile_row_bytes + block_rows * block_row_bytes (+ the molecule

@@ -1,9 +1,9 @@
-"""The default work budget: min(24 GiB, free device memory / 4).  The working buffers
-that the engine keeps from a previous build (tiles, blocks, operands) count as
-available, since the next build reuses or regrows them, so a build planned beside
-them gets the plan of a lone build.  Under memory pressure (a filler tensor leaves
-48 GB free) the budget binds, and the second of two identical builds must tile r1
-like the first and give the same bits.
+"""The default work budget: min(24 GiB, free device memory / 4).  The free memory a
+build sees excludes the working buffers the engine keeps from its previous build, so
+a build of the same shape as the last one takes that build's plan (and buffers)
+again.  Under memory pressure (a filler tensor leaves 48 GB free) the budget binds:
+the second of two identical builds must tile r1 like the first and give the same
+bits, and cutc_plan must report that plan beside the first build's buffers.
 """
 import numpy as np
 import pytest
@@ -25,7 +25,7 @@ def test_default_budget_counts_the_engines_working_buffers():
     filler = torch.empty(free - keep, dtype=torch.uint8, device="cuda")
     try:
         # 2.97 MB per r1 row in a tile: a 12 GiB budget takes two tiles of 4300 rows; a
-        # budget that did not count the first build's 14 GB of buffers would take three
+        # budget from the free memory beside the first build's 14 GB of buffers, three
         p = synth.make_problem(n_nuc=4, n_ao=40, n_grid1=8600, n_grid2=40000, size_bh=6, seed=5)
         args = (p.n_grid1, p.n_grid2, p.n_ao, p.n_nuc, cg.SPLIT_BF16, 5)
         lone = cg.plan(*args)
